@@ -1,0 +1,258 @@
+// kernels_bottom.cu -- coarsest-level solve in one CTA, FP64.
+//
+// Restates AMReX MLMG's bottom step as Alamo configures it
+// (Solver/Nonlocal/Linear.H:258 selects BiCGStab):
+//   cor = 0; BiCGStab on the diagonally scaled system (MLCGSolver::solve_bicgstab
+//   with Operator<Node>::normalize = divide by the diagonal, Operator.cpp:156-165);
+//   a failed solve (anything but a clean convergence) zeroes the correction;
+//   then `bottom_smooth` (after success) or `final_smooth` (after failure)
+//   Fsmooth calls of 2 damped-Jacobi sweeps each.
+// Every loop is bounded by maxiter / the smoothing counts; there is no
+// spin-wait.  The return code lands in ret_slot: 0 converged, 1-4 breakdown,
+// 8 not converged in maxiter.
+#include <cuda_runtime.h>
+
+#include "agb_internal.h"
+#include "stencil.cuh"
+
+namespace agb {
+
+constexpr int BOT_THREADS = 512;
+
+__device__ __forceinline__ double blk_sum(double v, double* red)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    double t = 0;
+    if (threadIdx.x < 32) {
+        t = threadIdx.x < (BOT_THREADS / 32) ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (threadIdx.x == 0) red[32] = t;
+    }
+    __syncthreads();
+    return red[32];
+}
+
+__device__ __forceinline__ double blk_max(double v, double* red)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) {
+        double w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = (w > v || w != w) ? w : v;
+    }
+    __syncthreads();
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double t = threadIdx.x < (BOT_THREADS / 32) ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) {
+            double w = __shfl_xor_sync(0xffffffffu, t, o);
+            t = (w > t || w != w) ? w : t;
+        }
+        if (threadIdx.x == 0) red[32] = t;
+    }
+    __syncthreads();
+    return red[32];
+}
+
+struct BotAcc {
+    const double* x;
+    const double* c;
+    long long S;
+    long long base;
+    long long o[3][3];
+    __device__ __forceinline__ long long off(int di, int dj, int dk) const
+    {
+        return base + o[0][di + 1] + o[1][dj + 1] + o[2][dk + 1];
+    }
+    __device__ __forceinline__ double u(int p, int di, int dj, int dk) const { return x[p * S + off(di, dj, dk)]; }
+    __device__ __forceinline__ double C(int m, int di, int dj, int dk) const { return c[m * S + off(di, dj, dk)]; }
+};
+
+// y = A x over all nodes of the level (threads stride over nodes)
+template <int SYM>
+__device__ void cta_apply(const LevelDesc& L, const BCTable& bc, const Geo<double>& g, int uniform,
+                          const double* ddw, const double* x, double* y)
+{
+    const long long cnt = L.count();
+    const long long st[3] = {1, (long long)L.P, (long long)L.P * L.nn[1]};
+    for (long long e = threadIdx.x; e < cnt; e += blockDim.x) {
+        const int i = (int)(e % L.nn[0]);
+        const int j = (int)((e / L.nn[0]) % L.nn[1]);
+        const int k = (int)(e / ((long long)L.nn[0] * L.nn[1]));
+        const int pos[3] = {i, j, k};
+        BotAcc acc;
+        acc.x = x;
+        acc.c = ddw;
+        acc.S = L.S;
+        acc.base = L.idx(i, j, k);
+        int mn[3], mx[3];
+        bool bnd = false;
+        for (int d = 0; d < 3; d++) {
+            mn[d] = !L.per[d] && pos[d] == 0;
+            mx[d] = !L.per[d] && pos[d] == L.n[d];
+            bnd = bnd || mn[d] || mx[d];
+            acc.o[d][0] = -st[d];
+            acc.o[d][1] = 0;
+            acc.o[d][2] = st[d];
+            if (L.per[d]) {
+                if (pos[d] == 0) acc.o[d][0] = st[d] * (L.n[d] - 1);
+                if (pos[d] == L.n[d] - 1) acc.o[d][2] = -st[d] * (L.n[d] - 1);
+            }
+        }
+        double f[3];
+        if (bnd) boundary_row<double, SYM>(acc, g, bc, mn, mx, f);
+        else interior_row<double, SYM>(acc, g, uniform != 0, f);
+        for (int c = 0; c < 3; c++) y[c * L.S + acc.base] = f[c];
+    }
+}
+
+#define FOR_NODES(q)                                                                                     \
+    for (long long e_ = threadIdx.x; e_ < cnt; e_ += blockDim.x)                                         \
+        for (int c_ = 0, i_ = (int)(e_ % L.nn[0]), j_ = (int)((e_ / L.nn[0]) % L.nn[1]),                  \
+                 k_ = (int)(e_ / ((long long)L.nn[0] * L.nn[1]));                                        \
+             c_ < 3; c_++)                                                                               \
+            for (long long q = c_ * L.S + L.idx(i_, j_, k_), once_ = 0; once_ < 1; once_++)
+
+template <typename T, int SYM>
+__global__ void __launch_bounds__(BOT_THREADS) k_bottom(LevelDesc L, BCTable bc, Geo<double> g, int uniform,
+                                                        const double* __restrict__ ddw,
+                                                        const double* __restrict__ diag, T* __restrict__ cor,
+                                                        const T* __restrict__ res, double* __restrict__ work,
+                                                        int maxiter, double eps_rel, double eps_abs, int nub,
+                                                        int nuf, double omega, int* ret_slot)
+{
+    __shared__ double red[33];
+    const long long n3 = 3 * L.S, cnt = L.count();
+    double *r = work, *rh = work + n3, *p = work + 2 * n3, *v = work + 3 * n3, *s = work + 4 * n3,
+           *t = work + 5 * n3, *sol = work + 6 * n3, *b = work + 7 * n3;
+
+    // r = (b - A*0)/D, sol = 0
+    double lm = 0;
+    FOR_NODES(q)
+    {
+        b[q] = (double)res[q];
+        sol[q] = 0.0;
+        r[q] = b[q] / diag[q];
+        rh[q] = r[q];
+        const double a = fabs(r[q]);
+        lm = (a > lm || a != a) ? a : lm;
+    }
+    double rnorm = blk_max(lm, red);
+    const double rnorm0 = rnorm;
+    int ret = 0;
+    double rho_1 = 0, alpha = 0, om = 0;
+    if (!(rnorm0 == 0 || rnorm0 < eps_abs)) {
+        for (int iter = 1; iter <= maxiter; iter++) {
+            double acc = 0;
+            FOR_NODES(q) acc += rh[q] * r[q];
+            const double rho = blk_sum(acc, red);
+            if (rho == 0) { ret = 1; break; }
+            if (iter == 1) {
+                FOR_NODES(q) p[q] = r[q];
+            } else {
+                const double beta = (rho / rho_1) * (alpha / om);
+                FOR_NODES(q) p[q] = r[q] + beta * (p[q] - om * v[q]);
+            }
+            __syncthreads();
+            cta_apply<SYM>(L, bc, g, uniform, ddw, p, v);
+            __syncthreads();
+            acc = 0;
+            FOR_NODES(q)
+            {
+                v[q] /= diag[q];
+                acc += rh[q] * v[q];
+            }
+            const double rhTv = blk_sum(acc, red);
+            if (rhTv != 0) alpha = rho / rhTv;
+            else { ret = 2; break; }
+            lm = 0;
+            FOR_NODES(q)
+            {
+                sol[q] += alpha * p[q];
+                s[q] = r[q] - alpha * v[q];
+                const double a = fabs(s[q]);
+                lm = (a > lm || a != a) ? a : lm;
+            }
+            rnorm = blk_max(lm, red);
+            if (rnorm < eps_rel * rnorm0 || rnorm < eps_abs) break;
+            cta_apply<SYM>(L, bc, g, uniform, ddw, s, t);
+            __syncthreads();
+            double tt = 0, ts = 0;
+            FOR_NODES(q)
+            {
+                t[q] /= diag[q];
+                tt += t[q] * t[q];
+                ts += t[q] * s[q];
+            }
+            tt = blk_sum(tt, red);
+            ts = blk_sum(ts, red);
+            if (tt != 0) om = ts / tt;
+            else { ret = 3; break; }
+            lm = 0;
+            FOR_NODES(q)
+            {
+                sol[q] += om * s[q];
+                r[q] = s[q] - om * t[q];
+                const double a = fabs(r[q]);
+                lm = (a > lm || a != a) ? a : lm;
+            }
+            rnorm = blk_max(lm, red);
+            if (rnorm < eps_rel * rnorm0 || rnorm < eps_abs) break;
+            if (om == 0) { ret = 4; break; }
+            rho_1 = rho;
+        }
+        if (ret == 0 && rnorm > eps_rel * rnorm0 && rnorm > eps_abs) ret = 8;
+        if (!((ret == 0 || ret == 8) && rnorm < rnorm0)) {
+            FOR_NODES(q) sol[q] = 0.0;
+        }
+        // MLMG::actualBottomSolve: anything but a clean solve discards the correction
+        if (ret != 0) {
+            FOR_NODES(q) sol[q] = 0.0;
+        }
+    }
+    __syncthreads();
+    // post-smoothing: Fsmooth = 2 Jacobi sweeps each
+    const int nsm = 2 * ((ret == 0) ? nub : nuf);
+    for (int sw = 0; sw < nsm; sw++) {
+        cta_apply<SYM>(L, bc, g, uniform, ddw, sol, t);
+        __syncthreads();
+        FOR_NODES(q)
+        {
+            const double Rx = t[q] - sol[q] * diag[q];
+            s[q] = (1. - omega) * sol[q] + omega * (b[q] - Rx) / diag[q];
+        }
+        __syncthreads();
+        FOR_NODES(q) sol[q] = s[q];
+        __syncthreads();
+    }
+    FOR_NODES(q) cor[q] = (T)sol[q];
+    if (threadIdx.x == 0 && ret_slot) *ret_slot = ret;
+}
+
+template <typename T>
+void launch_bottom(cudaStream_t st, int sym, const LevelDesc& L, const BCTable& bc, bool uniform, const double* ddw64,
+                   const double* diag64, T* cor, const T* res, double* work, int maxiter, double tol_rel,
+                   double tol_abs, int* ret_slot, int nub, int nuf, double omega)
+{
+    const Geo<double> g = make_geo<double>(L);
+    if (sym == SYM_ISO)
+        k_bottom<T, SYM_ISO><<<1, BOT_THREADS, 0, st>>>(L, bc, g, uniform ? 1 : 0, ddw64, diag64, cor, res, work,
+                                                        maxiter, tol_rel, tol_abs, nub, nuf, omega, ret_slot);
+    else
+        k_bottom<T, SYM_MM><<<1, BOT_THREADS, 0, st>>>(L, bc, g, uniform ? 1 : 0, ddw64, diag64, cor, res, work,
+                                                       maxiter, tol_rel, tol_abs, nub, nuf, omega, ret_slot);
+    count_launch();
+}
+
+template void launch_bottom<double>(cudaStream_t, int, const LevelDesc&, const BCTable&, bool, const double*,
+                                    const double*, double*, const double*, double*, int, double, double, int*, int,
+                                    int, double);
+template void launch_bottom<float>(cudaStream_t, int, const LevelDesc&, const BCTable&, bool, const double*,
+                                   const double*, float*, const float*, double*, int, double, double, int*, int, int,
+                                   double);
+
+}  // namespace agb

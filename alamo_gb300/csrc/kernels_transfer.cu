@@ -1,0 +1,329 @@
+// kernels_transfer.cu -- inter-level transfers and vector kernels.
+//
+//   restriction       Operator<Node>::restriction, Operator/Operator.cpp:262-363
+//   interpolation     Operator<Node>::interpolation (additive), Operator.cpp:365-434;
+//                     `assign` variant = MLMG interpAssign used by the F-cycle
+//   average_ddw       Elastic::averageDownCoeffsSameAmrLevel, Operator/Elastic.cpp:748-910
+//   import / export   reference nodal-box images (n+1 nodes per direction, SoA
+//                     MultiFab components or AoS BaseFab<Matrix4>) <-> padded storage
+#include <cuda_runtime.h>
+
+#include "agb_internal.h"
+
+namespace agb {
+
+__device__ __forceinline__ int wrapn(int i, int n, int per)
+{
+    if (per) {
+        if (i < 0) return i + n;
+        if (i >= n) return i - n;
+    }
+    return i;
+}
+
+static inline dim3 grid_for(const LevelDesc& L, dim3 blk)
+{
+    return dim3((L.nn[0] + blk.x - 1) / blk.x, (L.nn[1] + blk.y - 1) / blk.y, (L.nn[2] + blk.z - 1) / blk.z);
+}
+
+// Nodal full weighting with lower-dimensional stencils on the coarse domain
+// boundary; the same weights serve the residual restriction and the modulus
+// averaging.  F(a,b,c) returns the fine value at (2I+a, 2J+b, 2K+c).
+template <typename T, class F>
+__device__ __forceinline__ T full_weight(const F& f, bool bI, bool bJ, bool bK)
+{
+    if (bI && bJ && bK) return f(0, 0, 0);
+    if (bJ && bK) return (T)0.25 * f(-1, 0, 0) + (T)0.5 * f(0, 0, 0) + (T)0.25 * f(1, 0, 0);
+    if (bK && bI) return (T)0.25 * f(0, -1, 0) + (T)0.5 * f(0, 0, 0) + (T)0.25 * f(0, 1, 0);
+    if (bI && bJ) return (T)0.25 * f(0, 0, -1) + (T)0.5 * f(0, 0, 0) + (T)0.25 * f(0, 0, 1);
+    if (bI)
+        return (f(0, -1, -1) + (T)2 * f(0, 0, -1) + f(0, 1, -1) + (T)2 * f(0, -1, 0) + (T)4 * f(0, 0, 0) +
+                (T)2 * f(0, 1, 0) + f(0, -1, 1) + (T)2 * f(0, 0, 1) + f(0, 1, 1)) * (T)(1.0 / 16.0);
+    if (bJ)
+        return (f(-1, 0, -1) + (T)2 * f(-1, 0, 0) + f(-1, 0, 1) + (T)2 * f(0, 0, -1) + (T)4 * f(0, 0, 0) +
+                (T)2 * f(0, 0, 1) + f(1, 0, -1) + (T)2 * f(1, 0, 0) + f(1, 0, 1)) * (T)(1.0 / 16.0);
+    if (bK)
+        return (f(-1, -1, 0) + (T)2 * f(0, -1, 0) + f(1, -1, 0) + (T)2 * f(-1, 0, 0) + (T)4 * f(0, 0, 0) +
+                (T)2 * f(1, 0, 0) + f(-1, 1, 0) + (T)2 * f(0, 1, 0) + f(1, 1, 0)) * (T)(1.0 / 16.0);
+    return (f(-1, -1, -1) + f(-1, -1, 1) + f(-1, 1, -1) + f(-1, 1, 1) + f(1, -1, -1) + f(1, -1, 1) + f(1, 1, -1) +
+            f(1, 1, 1)) * (T)(1.0 / 64.0) +
+           (f(0, -1, -1) + f(0, -1, 1) + f(0, 1, -1) + f(0, 1, 1) + f(-1, 0, -1) + f(1, 0, -1) + f(-1, 0, 1) +
+            f(1, 0, 1) + f(-1, -1, 0) + f(-1, 1, 0) + f(1, -1, 0) + f(1, 1, 0)) * (T)(1.0 / 32.0) +
+           (f(-1, 0, 0) + f(0, -1, 0) + f(0, 0, -1) + f(1, 0, 0) + f(0, 1, 0) + f(0, 0, 1)) * (T)(1.0 / 16.0) +
+           f(0, 0, 0) * (T)(1.0 / 8.0);
+}
+
+template <typename T>
+__global__ void k_restrict(LevelDesc Lf, LevelDesc Lc, const T* __restrict__ fine, T* __restrict__ crse, int ncomp)
+{
+    const int I = blockIdx.x * blockDim.x + threadIdx.x;
+    const int J = blockIdx.y * blockDim.y + threadIdx.y;
+    const int K = blockIdx.z * blockDim.z + threadIdx.z;
+    if (I >= Lc.nn[0] || J >= Lc.nn[1] || K >= Lc.nn[2]) return;
+    const bool bI = !Lc.per[0] && (I == 0 || I == Lc.n[0]);
+    const bool bJ = !Lc.per[1] && (J == 0 || J == Lc.n[1]);
+    const bool bK = !Lc.per[2] && (K == 0 || K == Lc.n[2]);
+    const long long q = Lc.idx(I, J, K);
+    for (int c = 0; c < ncomp; c++) {
+        const T* src = fine + c * Lf.S;
+        auto f = [&](int a, int b, int d) -> T {
+            return __ldg(src + Lf.idx(wrapn(2 * I + a, Lf.n[0], Lf.per[0]), wrapn(2 * J + b, Lf.n[1], Lf.per[1]),
+                                      wrapn(2 * K + d, Lf.n[2], Lf.per[2])));
+        };
+        crse[c * Lc.S + q] = full_weight<T>(f, bI, bJ, bK);
+    }
+}
+
+template <typename T>
+__global__ void k_interp(LevelDesc Lf, LevelDesc Lc, T* __restrict__ fine, const T* __restrict__ crse, int assign)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    if (i >= Lf.nn[0] || j >= Lf.nn[1] || k >= Lf.nn[2]) return;
+    const int I = i >> 1, J = j >> 1, K = k >> 1;
+    const int I1 = wrapn(I + 1, Lc.n[0], Lc.per[0]), J1 = wrapn(J + 1, Lc.n[1], Lc.per[1]),
+              K1 = wrapn(K + 1, Lc.n[2], Lc.per[2]);
+    const bool ei = !(i & 1), ej = !(j & 1), ek = !(k & 1);
+    const long long q = Lf.idx(i, j, k);
+    for (int c = 0; c < 3; c++) {
+        const T* cs = crse + c * Lc.S;
+        auto C = [&](int a, int b, int d) -> T { return __ldg(cs + Lc.idx(a ? I1 : I, b ? J1 : J, d ? K1 : K)); };
+        T t;
+        if (ei && ej && ek) t = C(0, 0, 0);
+        else if (ej && ek) t = (T)0.5 * (C(0, 0, 0) + C(1, 0, 0));
+        else if (ek && ei) t = (T)0.5 * (C(0, 0, 0) + C(0, 1, 0));
+        else if (ei && ej) t = (T)0.5 * (C(0, 0, 0) + C(0, 0, 1));
+        else if (ei) t = (T)0.25 * (C(0, 0, 0) + C(0, 1, 0) + C(0, 0, 1) + C(0, 1, 1));
+        else if (ej) t = (T)0.25 * (C(0, 0, 0) + C(0, 0, 1) + C(1, 0, 0) + C(1, 0, 1));
+        else if (ek) t = (T)0.25 * (C(0, 0, 0) + C(1, 0, 0) + C(0, 1, 0) + C(1, 1, 0));
+        else
+            t = (T)0.125 * (C(0, 0, 0) + C(1, 0, 0) + C(0, 1, 0) + C(0, 0, 1) + C(0, 1, 1) + C(1, 0, 1) +
+                            C(1, 1, 0) + C(1, 1, 1));
+        T* o = fine + c * Lf.S + q;
+        *o = assign ? t : (*o + t);
+    }
+}
+
+template <typename T>
+__global__ void k_avg_ddw(LevelDesc Lf, LevelDesc Lc, const T* __restrict__ fine, T* __restrict__ crse, int ncoef)
+{
+    const int I = blockIdx.x * blockDim.x + threadIdx.x;
+    const int J = blockIdx.y * blockDim.y + threadIdx.y;
+    const int K = blockIdx.z * blockDim.z + threadIdx.z;
+    if (I >= Lc.nn[0] || J >= Lc.nn[1] || K >= Lc.nn[2]) return;
+    const bool bI = !Lc.per[0] && (I == 0 || I == Lc.n[0]);
+    const bool bJ = !Lc.per[1] && (J == 0 || J == Lc.n[1]);
+    const bool bK = !Lc.per[2] && (K == 0 || K == Lc.n[2]);
+    const long long q = Lc.idx(I, J, K);
+    for (int m = 0; m < ncoef; m++) {
+        const T* src = fine + m * Lf.S;
+        auto f = [&](int a, int b, int d) -> T {
+            return src[Lf.idx(wrapn(2 * I + a, Lf.n[0], Lf.per[0]), wrapn(2 * J + b, Lf.n[1], Lf.per[1]),
+                              wrapn(2 * K + d, Lf.n[2], Lf.per[2]))];
+        };
+        crse[m * Lc.S + q] = full_weight<T>(f, bI, bJ, bK);
+    }
+}
+
+template <typename TD, typename TS>
+__global__ void k_convert(long long n, const TS* __restrict__ src, TD* __restrict__ dst, double scale)
+{
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
+        dst[e] = (TD)((double)src[e] * scale);
+}
+
+template <typename T>
+__global__ void k_axpy(long long n, T* __restrict__ y, const T* __restrict__ x, T a)
+{
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
+        y[e] += a * x[e];
+}
+
+template <typename T> struct MaxSlot;
+template <> struct MaxSlot<double> {
+    static __device__ void put(void* s, double v) { atomicMax((unsigned long long*)s, (unsigned long long)__double_as_longlong(v)); }
+};
+template <> struct MaxSlot<float> {
+    static __device__ void put(void* s, float v) { atomicMax((unsigned int*)s, __float_as_uint(v)); }
+};
+
+template <typename T>
+__global__ void k_norm_inf(long long n, const T* __restrict__ x, void* slot)
+{
+    T m = 0;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const T a = fabs(x[e]);
+        m = (a > m || a != a) ? a : m;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const T w = __shfl_xor_sync(0xffffffffu, m, o);
+        m = (w > m || w != w) ? w : m;
+    }
+    if ((threadIdx.x & 31) == 0) MaxSlot<T>::put(slot, m);
+}
+
+// Reference nodal box (n+1 nodes per direction) -> padded storage, for the
+// k-planes [k0, k0+kc).  With `chunk`, src holds only those planes (a staging
+// slab); otherwise src is the whole box.
+template <typename TD, typename TS>
+__global__ void k_import(LevelDesc L, int ncomp, const TS* __restrict__ src, TD* __restrict__ dst, int aos, int k0,
+                         int kc, int chunk)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = k0 + blockIdx.z * blockDim.z + threadIdx.z;
+    if (i >= L.nn[0] || j >= L.nn[1] || k >= L.nn[2] || k >= k0 + kc) return;
+    const long long planeN = (long long)(L.n[0] + 1) * (L.n[1] + 1);
+    const long long Nsrc = chunk ? planeN * kc : planeN * (L.n[2] + 1);
+    const long long s = (long long)i + (long long)(L.n[0] + 1) * j + planeN * (chunk ? k - k0 : k);
+    const long long q = L.idx(i, j, k);
+    for (int c = 0; c < ncomp; c++) dst[c * L.S + q] = (TD)(aos ? src[s * ncomp + c] : src[c * Nsrc + s]);
+}
+
+// padded storage -> reference nodal box for planes [k0, k0+kc) (periodic images filled)
+template <typename TD, typename TS>
+__global__ void k_export(LevelDesc L, int ncomp, const TS* __restrict__ src, TD* __restrict__ dst, int aos, int k0,
+                         int kc, int chunk)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = k0 + blockIdx.z * blockDim.z + threadIdx.z;
+    if (i > L.n[0] || j > L.n[1] || k > L.n[2] || k >= k0 + kc) return;
+    const long long planeN = (long long)(L.n[0] + 1) * (L.n[1] + 1);
+    const long long Ndst = chunk ? planeN * kc : planeN * (L.n[2] + 1);
+    const long long s = (long long)i + (long long)(L.n[0] + 1) * j + planeN * (chunk ? k - k0 : k);
+    const int ii = (L.per[0] && i == L.n[0]) ? 0 : i;
+    const int jj = (L.per[1] && j == L.n[1]) ? 0 : j;
+    const int kk = (L.per[2] && k == L.n[2]) ? 0 : k;
+    const long long q = L.idx(ii, jj, kk);
+    for (int c = 0; c < ncomp; c++) {
+        const TD v = (TD)src[c * L.S + q];
+        if (aos) dst[s * ncomp + c] = v;
+        else dst[c * Ndst + s] = v;
+    }
+}
+
+// y += a * x with x in FP32, y in FP64 (refinement accumulation)
+__global__ void k_axpy_mixed(long long n, double* __restrict__ y, const float* __restrict__ x, double a)
+{
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
+        y[e] += a * (double)x[e];
+}
+
+template <typename TD>
+__global__ void k_recip(long long n, const double* __restrict__ d, TD* __restrict__ r)
+{
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
+        r[e] = d[e] != 0.0 ? (TD)(1.0 / d[e]) : (TD)0;
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+static inline int blocks_1d(long long n)
+{
+    long long b = (n + 255) / 256;
+    return (int)(b < 152 * 16 ? (b < 1 ? 1 : b) : 152 * 16);
+}
+
+template <typename T>
+void launch_restriction(cudaStream_t st, const LevelDesc& Lf, const LevelDesc& Lc, const T* fine, T* crse, int ncomp)
+{
+    dim3 blk(32, 4, 2);
+    k_restrict<T><<<grid_for(Lc, blk), blk, 0, st>>>(Lf, Lc, fine, crse, ncomp); count_launch();
+}
+
+template <typename T>
+void launch_interpolation(cudaStream_t st, const LevelDesc& Lf, const LevelDesc& Lc, T* fine, const T* crse,
+                          bool assign)
+{
+    dim3 blk(32, 4, 2);
+    k_interp<T><<<grid_for(Lf, blk), blk, 0, st>>>(Lf, Lc, fine, crse, assign ? 1 : 0); count_launch();
+}
+
+template <typename T>
+void launch_average_ddw(cudaStream_t st, const LevelDesc& Lf, const LevelDesc& Lc, const T* fine, T* crse, int ncoef)
+{
+    dim3 blk(32, 4, 2);
+    k_avg_ddw<T><<<grid_for(Lc, blk), blk, 0, st>>>(Lf, Lc, fine, crse, ncoef); count_launch();
+}
+
+template <typename TD, typename TS>
+void launch_convert(cudaStream_t st, const LevelDesc& L, int ncomp, const TS* src, TD* dst, double scale)
+{
+    const long long n = (long long)ncomp * L.S;
+    k_convert<TD, TS><<<blocks_1d(n), 256, 0, st>>>(n, src, dst, scale); count_launch();
+}
+
+template <typename T>
+void launch_axpy(cudaStream_t st, const LevelDesc& L, int ncomp, T* y, const T* x, T a)
+{
+    const long long n = (long long)ncomp * L.S;
+    k_axpy<T><<<blocks_1d(n), 256, 0, st>>>(n, y, x, a); count_launch();
+}
+
+template <typename T>
+void launch_zero(cudaStream_t st, const LevelDesc& L, int ncomp, T* y)
+{
+    cudaMemsetAsync(y, 0, sizeof(T) * (size_t)ncomp * (size_t)L.S, st);
+}
+
+template <typename T>
+void launch_norm_inf(cudaStream_t st, const LevelDesc& L, int ncomp, const T* x, void* slot)
+{
+    const long long n = (long long)ncomp * L.S;
+    k_norm_inf<T><<<blocks_1d(n), 256, 0, st>>>(n, x, slot); count_launch();
+}
+
+template <typename TD, typename TS>
+void launch_import(cudaStream_t st, const LevelDesc& L, int ncomp, const TS* src, TD* dst, bool aos, int k0, int kc,
+                   bool chunk)
+{
+    dim3 blk(32, 4, 2);
+    dim3 grd((L.nn[0] + blk.x - 1) / blk.x, (L.nn[1] + blk.y - 1) / blk.y, (kc + blk.z - 1) / blk.z);
+    k_import<TD, TS><<<grd, blk, 0, st>>>(L, ncomp, src, dst, aos ? 1 : 0, k0, kc, chunk ? 1 : 0); count_launch();
+}
+
+template <typename TD, typename TS>
+void launch_export(cudaStream_t st, const LevelDesc& L, int ncomp, const TS* src, TD* dst, bool aos, int k0, int kc,
+                   bool chunk)
+{
+    dim3 blk(32, 4, 2);
+    dim3 grd((L.n[0] + 1 + blk.x - 1) / blk.x, (L.n[1] + 1 + blk.y - 1) / blk.y, (kc + blk.z - 1) / blk.z);
+    k_export<TD, TS><<<grd, blk, 0, st>>>(L, ncomp, src, dst, aos ? 1 : 0, k0, kc, chunk ? 1 : 0); count_launch();
+}
+
+void launch_axpy_mixed(cudaStream_t st, const LevelDesc& L, int ncomp, double* y, const float* x, double a)
+{
+    const long long n = (long long)ncomp * L.S;
+    k_axpy_mixed<<<blocks_1d(n), 256, 0, st>>>(n, y, x, a); count_launch();
+}
+
+template <typename TD>
+void launch_recip(cudaStream_t st, const LevelDesc& L, int ncomp, const double* d, TD* r)
+{
+    const long long n = (long long)ncomp * L.S;
+    k_recip<TD><<<blocks_1d(n), 256, 0, st>>>(n, d, r); count_launch();
+}
+
+#define INST(T)                                                                                              \
+    template void launch_restriction<T>(cudaStream_t, const LevelDesc&, const LevelDesc&, const T*, T*, int); \
+    template void launch_interpolation<T>(cudaStream_t, const LevelDesc&, const LevelDesc&, T*, const T*, bool); \
+    template void launch_average_ddw<T>(cudaStream_t, const LevelDesc&, const LevelDesc&, const T*, T*, int); \
+    template void launch_axpy<T>(cudaStream_t, const LevelDesc&, int, T*, const T*, T);                      \
+    template void launch_zero<T>(cudaStream_t, const LevelDesc&, int, T*);                                   \
+    template void launch_norm_inf<T>(cudaStream_t, const LevelDesc&, int, const T*, void*);                  \
+    template void launch_recip<T>(cudaStream_t, const LevelDesc&, int, const double*, T*);                   \
+    template void launch_import<T, double>(cudaStream_t, const LevelDesc&, int, const double*, T*, bool, int, int, bool); \
+    template void launch_import<T, float>(cudaStream_t, const LevelDesc&, int, const float*, T*, bool, int, int, bool);   \
+    template void launch_export<T, double>(cudaStream_t, const LevelDesc&, int, const double*, T*, bool, int, int, bool); \
+    template void launch_export<T, float>(cudaStream_t, const LevelDesc&, int, const float*, T*, bool, int, int, bool);
+INST(double)
+INST(float)
+#undef INST
+template void launch_convert<float, double>(cudaStream_t, const LevelDesc&, int, const double*, float*, double);
+template void launch_convert<double, float>(cudaStream_t, const LevelDesc&, int, const float*, double*, double);
+template void launch_convert<double, double>(cudaStream_t, const LevelDesc&, int, const double*, double*, double);
+
+}  // namespace agb

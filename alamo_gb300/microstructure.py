@@ -1,0 +1,131 @@
+"""Seeded synthetic microstructures for the benchmark workloads.
+
+No public dataset is involved; every field is generated from a SplitMix64
+stream so that runs are reproducible on any host.
+
+    sphere_inclusion   isotropic matrix with a smoothed spherical inclusion and
+                       an eigenstrain inside it (65^3-node workload)
+    voronoi_cubic      cubic-anisotropic polycrystal: Voronoi grains with
+                       uniformly random orientations (257^3-node workload)
+    cubic              Matrix4<3,MajorMinor>::Cubic(C11, C12, C44, R)
+                       (Set/Matrix4_MajorMinor.H:518-547), including its slot
+                       aliasing: the stored value of each of the 21 slots is the
+                       rotated non-minor-symmetric tensor at the last (p,q,s,t)
+                       of the reference's loop that maps to the slot.
+"""
+import itertools
+
+import numpy as np
+
+_MASK = (1 << 64) - 1
+
+
+class SplitMix64:
+    def __init__(self, seed):
+        self.s = int(seed) & _MASK
+
+    def next_u64(self):
+        self.s = (self.s + 0x9E3779B97F4A7C15) & _MASK
+        z = self.s
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & _MASK
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & _MASK
+        return z ^ (z >> 31)
+
+    def uniform(self, n=None):
+        if n is None:
+            return (self.next_u64() >> 11) * (1.0 / (1 << 53))
+        return np.array([(self.next_u64() >> 11) * (1.0 / (1 << 53)) for _ in range(n)])
+
+    def normal(self):
+        u1 = max(self.uniform(), 1e-300)
+        u2 = self.uniform()
+        return np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * np.pi * u2)
+
+
+def _mm_slot_table():
+    groups = [[0], [27, 9, 3, 1], [54, 18, 6, 2], [36, 4], [63, 45, 7, 5], [72, 8], [30, 12, 28, 10],
+              [57, 21, 33, 15, 55, 19, 29, 11], [39, 37, 31, 13], [66, 48, 64, 46, 34, 16, 32, 14],
+              [75, 73, 35, 17], [60, 24, 56, 20], [42, 58, 22, 38], [69, 51, 61, 25, 65, 47, 59, 23],
+              [78, 74, 62, 26], [40], [67, 49, 43, 41], [76, 44], [70, 52, 68, 50], [79, 77, 71, 53], [80]]
+    t = {}
+    for slot, uids in enumerate(groups):
+        for u in uids:
+            t[u] = slot
+    return t
+
+
+_SLOT = _mm_slot_table()
+
+
+def quat_to_rot(q):
+    """Rotation matrix of the normalised quaternion (w, x, y, z)."""
+    w, x, y, z = np.asarray(q, dtype=np.float64) / np.linalg.norm(q)
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)],
+                     [2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)],
+                     [2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)]])
+
+
+def cubic(C11, C12, C44, R=None):
+    R = np.eye(3) if R is None else np.asarray(R, dtype=np.float64)
+    Ct = np.zeros((3, 3, 3, 3))
+    for i, j, k, l in itertools.product(range(3), repeat=4):
+        if i == j == k == l:
+            Ct[i, j, k, l] = C11
+        elif i == k and j == l:
+            Ct[i, j, k, l] = C44
+        elif i == j and k == l:
+            Ct[i, j, k, l] = C12
+    full = np.einsum("pi,sk,ijkl,qj,tl->pqst", R, R, Ct, R, R)
+    out = np.zeros(21)
+    for p, q, s, t in itertools.product(range(3), repeat=4):
+        out[_SLOT[p + 3 * q + 9 * s + 27 * t]] = full[p, q, s, t]
+    return out
+
+
+def node_coords(n, lo=0.0, hi=1.0):
+    return lo + (hi - lo) * np.arange(n + 1) / n
+
+
+def sphere_inclusion(n=64, radius=0.25, lam_m=1.0, mu_m=1.0, lam_i=10.0, mu_i=10.0, eig=1e-3):
+    """Isotropic matrix + smoothed sphere (eta = (1 - tanh((r-R)/(2 dx)))/2).
+    Returns (ddw AoS (lambda, mu) per node, F0 AoS 9 per node) on (n+1)^3 nodes."""
+    x = node_coords(n)
+    dx = 1.0 / n
+    Z, Y, X = np.meshgrid(x, x, x, indexing="ij")
+    r = np.sqrt((X - 0.5) ** 2 + (Y - 0.5) ** 2 + (Z - 0.5) ** 2)
+    eta = 0.5 * (1.0 - np.tanh((r - radius) / (2.0 * dx)))
+    eta = eta.reshape(-1)
+    ddw = np.empty((eta.size, 2))
+    ddw[:, 0] = eta * lam_i + (1.0 - eta) * lam_m
+    ddw[:, 1] = eta * mu_i + (1.0 - eta) * mu_m
+    F0 = np.zeros((eta.size, 9))
+    F0[:, 0] = F0[:, 4] = F0[:, 8] = eta * eig
+    return ddw.reshape(-1), F0.reshape(-1)
+
+
+def voronoi_seeds(ngrains=64, seed=20260, C11=1.68, C12=1.21, C44=0.75):
+    rng = SplitMix64(seed)
+    pts = np.array([[rng.uniform() for _ in range(3)] for _ in range(ngrains)])
+    table = np.zeros((ngrains, 21))
+    for g in range(ngrains):
+        q = [rng.normal() for _ in range(4)]
+        table[g] = cubic(C11, C12, C44, quat_to_rot(q))
+    return pts, table
+
+
+def voronoi_grain_ids(n, pts):
+    """Nearest seed (Euclidean, non-periodic) of every node, int32, (n+1)^3."""
+    x = node_coords(n)
+    ids = np.empty((n + 1, n + 1, n + 1), np.int32)
+    YY, XX = np.meshgrid(x, x, indexing="ij")
+    for k in range(n + 1):
+        d2 = ((XX[..., None] - pts[:, 0]) ** 2 + (YY[..., None] - pts[:, 1]) ** 2 + (x[k] - pts[:, 2]) ** 2)
+        ids[k] = np.argmin(d2, axis=-1)
+    return ids.reshape(-1)
+
+
+def voronoi_cubic(n=256, ngrains=64, seed=20260, C11=1.68, C12=1.21, C44=0.75):
+    """Returns (ddw AoS 21 per node, grain ids, table)."""
+    pts, table = voronoi_seeds(ngrains, seed, C11, C12, C44)
+    ids = voronoi_grain_ids(n, pts)
+    return table[ids].reshape(-1), ids, table

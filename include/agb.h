@@ -1,0 +1,191 @@
+/*
+ * agb.h -- C ABI of alamo_gb300: a GB300 (sm_103a) implementation of Alamo's
+ * nodal linear-elastic multigrid solve, drop-in for the
+ * Operator::Elastic<SYM> / Solver::Nonlocal::Linear path.
+ *
+ * Conventions
+ *   - Every function returns agb_status; no C++ exception crosses the ABI.
+ *     agb_last_error() gives a thread-local message for the last failure.
+ *   - Field arguments are the memory image of the reference's single-box
+ *     nodal MultiFab of the level: (n0+1)(n1+1)(n2+1) nodes, i fastest, the
+ *     three components one after the other (SoA), FP64 unless the name ends in
+ *     _f32.  In periodic directions node n duplicates node 0 (inputs must keep
+ *     them equal; outputs do).
+ *   - Modulus fields (Set::Matrix4<3,SYM> per node) are AGB_LAYOUT_AOS, the
+ *     memory image of a BaseFab<Matrix4>: 2 doubles (lambda, mu) for
+ *     AGB_ISO, the 21 doubles of Matrix4<3,MajorMinor>::data for
+ *     AGB_MAJORMINOR; or AGB_LAYOUT_SOA (coefficient-major).
+ *   - `mem` says whether pointers are host (AGB_MEM_HOST) or device
+ *     (AGB_MEM_DEVICE) memory.  Host pointers may be pageable or pinned.
+ *   - One handle is not re-entrant; distinct handles may be used from
+ *     distinct host threads.  Each operator owns one CUDA stream; calls
+ *     return after their work has completed.
+ *   - The library owns every device buffer it uses.  There is no CPU
+ *     fallback: without a usable GPU every call returns AGB_CUDA.
+ *
+ * The reference interface each entry point replaces is cited beside it
+ * (paths relative to the alamo source tree).
+ */
+#ifndef AGB_H
+#define AGB_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    AGB_OK = 0,
+    AGB_MAXITER = 1,   /* max_iter reached before tol (MLMG "failed to converge") */
+    AGB_STALL = 2,     /* residual stopped decreasing */
+    AGB_NAN = 3,       /* NaN in a residual (Elastic.cpp:262-286 aborts on this) */
+    AGB_BADARG = 4,
+    AGB_CUDA = 5,      /* CUDA error or no usable device */
+    AGB_NOMEM = 6,
+    AGB_STATE = 7      /* call out of order (e.g. solve before set_model) */
+} agb_status;
+
+enum { AGB_ISO = 0, AGB_MAJORMINOR = 1 };                  /* Set::Sym::Isotropic, Set::Sym::MajorMinor */
+enum { AGB_MEM_HOST = 0, AGB_MEM_DEVICE = 1 };
+enum { AGB_LAYOUT_AOS = 0, AGB_LAYOUT_SOA = 1 };
+enum { AGB_PREC_F64 = 0, AGB_PREC_MIXED = 1 };
+
+/* BC::Operator::Elastic::Elastic::Type, BC/Operator/Elastic/Elastic.H:26 */
+enum { AGB_BC_DISP = 0, AGB_BC_TRAC = 1, AGB_BC_PERIODIC = 2, AGB_BC_NEUMANN = 3, AGB_BC_NONE = 4 };
+
+/* BC::Operator::Elastic::Elastic::Face (3D), BC/Operator/Elastic/Elastic.H:35-43 */
+#define AGB_NFACES 26
+enum {
+    AGB_XLO, AGB_YLO, AGB_ZLO, AGB_XHI, AGB_YHI, AGB_ZHI,
+    AGB_YLO_ZLO, AGB_YLO_ZHI, AGB_YHI_ZLO, AGB_YHI_ZHI,
+    AGB_ZLO_XLO, AGB_ZLO_XHI, AGB_ZHI_XLO, AGB_ZHI_XHI,
+    AGB_XLO_YLO, AGB_XLO_YHI, AGB_XHI_YLO, AGB_XHI_YHI,
+    AGB_XLO_YLO_ZLO, AGB_XLO_YLO_ZHI, AGB_XLO_YHI_ZLO, AGB_XLO_YHI_ZHI,
+    AGB_XHI_YLO_ZLO, AGB_XHI_YLO_ZHI, AGB_XHI_YHI_ZLO, AGB_XHI_YHI_ZHI
+};
+
+/* BC::Operator::Elastic::Constant state: m_bc_type / m_bc_val at the
+ * current time (Constant.H:435-436). */
+typedef struct {
+    int type[AGB_NFACES][3];
+    double val[AGB_NFACES][3];
+} agb_bc;
+
+/* Solver::Nonlocal::Linear parameters (Linear.H:231-250, 296-382) plus the
+ * mixed-precision controls. */
+typedef struct {
+    int max_iter;             /* MLMG max iterations (default 200) */
+    int fixed_iter;           /* <0 off */
+    int pre_smooth;           /* Fsmooth calls before restriction (each = 2 Jacobi sweeps), default 2 */
+    int post_smooth;          /* default 2 */
+    int final_smooth;         /* after a failed bottom solve, default 8 */
+    int bottom_smooth;        /* after a converged bottom solve, default 0 */
+    int max_fmg_iter;         /* iterations run as F-cycles; Linear.H:261 sets 1e8; 0 = V-cycles */
+    int bottom_max_iter;      /* default 200 */
+    double bottom_tol_rel;    /* default 1e-4 */
+    double bottom_tol_abs;    /* <0 off */
+    double omega;             /* Jacobi damping; < 0 (default) keeps the operator's, 2/3 (Operator.H:123) */
+    int max_coarsening_level; /* default 30 */
+    int verbose;
+    int precision;            /* AGB_PREC_F64 (plain) or AGB_PREC_MIXED (FP32 cycles in FP64 refinement) */
+    double inner_tol_rel;     /* mixed: residual reduction asked of each FP32 inner solve (default 1e-4) */
+    int inner_max_iter;       /* mixed: FP32 cycles per refinement step (default 60) */
+    int max_refine;           /* mixed: refinement steps (default 20) */
+    int use_graph;            /* replay each cycle from a captured CUDA graph (default 1) */
+} agb_solver_params;
+
+typedef struct {
+    int iterations;           /* MLMG cycles (plain) or FP32 cycles in total (mixed) */
+    int status;               /* agb_status of the solve */
+    double res0;              /* ||b - A x0||_inf (FP64) */
+    double res_final;         /* ||b - A x||_inf (FP64) at return */
+    double rhs_norm;          /* ||b||_inf */
+    int nlevels;
+    int refinements;          /* mixed: FP64 residual evaluations after the first */
+    double solve_ms;          /* device time of the solve (CUDA events on the operator stream) */
+    long long kernels;        /* kernels this library launched for the solve (graph replays included) */
+} agb_solve_report;
+
+typedef struct agb_op_s* agb_op;
+typedef struct agb_solver_s* agb_solver;
+
+void agb_default_params(agb_solver_params* p);
+const char* agb_last_error(void);
+const char* agb_version(void);
+
+/* Operator::Elastic<SYM>::Elastic(geom, grids, dmap, info) + define,
+ * Operator/Elastic.cpp:10-55; LPInfo max_coarsening_level sets the depth. */
+agb_status agb_op_create(const int n_cells[3], const double dx[3], const int periodic[3], int sym,
+                         int max_coarsening_level, agb_op* out);
+agb_status agb_op_destroy(agb_op op);
+/* Elastic::SetBC, Operator/Elastic.H:61-65 */
+agb_status agb_op_set_bc(agb_op op, const agb_bc* bc);
+/* Elastic::SetModel(amrlev, MultiTab), Operator/Elastic.cpp:89-116 (copies) */
+agb_status agb_op_set_model(agb_op op, const double* ddw, int layout, int mem);
+/* Elastic::SetUniform, Elastic.H:105 */
+agb_status agb_op_set_uniform(agb_op op, int uniform);
+/* Operator<Node>::SetOmega, Operator.H:57 */
+agb_status agb_op_set_omega(agb_op op, double omega);
+agb_status agb_op_num_levels(agb_op op, int* nlevels);
+agb_status agb_op_level_cells(agb_op op, int level, int n_cells[3]);
+/* Operator<Node>::prepareForSolve: averageDownCoeffs + Diagonal(true), Operator.cpp:253-260 */
+agb_status agb_op_prepare(agb_op op);
+/* modulus of a level after averaging (Elastic.cpp:748-910), for inspection */
+agb_status agb_op_get_model(agb_op op, int level, double* ddw, int layout, int mem);
+/* Elastic::Fapply(amrlev=0, mglev, f, u), Operator/Elastic.cpp:141-292 */
+agb_status agb_op_fapply(agb_op op, int level, double* f, const double* u, int mem);
+agb_status agb_op_fapply_f32(agb_op op, int level, float* f, const float* u, int mem);
+/* Elastic::Diagonal(amrlev=0, mglev, diag), Operator/Elastic.cpp:298-379 */
+agb_status agb_op_diagonal(agb_op op, int level, double* diag, int mem);
+/* Operator<Node>::Fsmooth(amrlev=0, mglev, x, b): 2 damped-Jacobi sweeps, Operator.cpp:88-154 */
+agb_status agb_op_fsmooth(agb_op op, int level, double* x, const double* b, int mem);
+agb_status agb_op_fsmooth_f32(agb_op op, int level, float* x, const float* b, int mem);
+/* Operator<Node>::solutionResidual: r = b - A x, Operator.cpp:636-645 */
+agb_status agb_op_residual(agb_op op, int level, double* r, const double* x, const double* b, int mem);
+/* Operator<Node>::restriction(amrlev, cmglev, crse, fine), Operator.cpp:262-363 */
+agb_status agb_op_restriction(agb_op op, int crse_level, double* crse, const double* fine, int mem);
+/* Operator<Node>::interpolation(amrlev, fmglev, fine, crse): fine += P crse, Operator.cpp:365-434 */
+agb_status agb_op_interpolation(agb_op op, int fine_level, double* fine, const double* crse, int mem);
+
+/* Solver::Nonlocal::Linear::Define(op), Linear.H:36-43 */
+agb_status agb_solver_create(agb_op op, const agb_solver_params* params, agb_solver* out);
+agb_status agb_solver_destroy(agb_solver s);
+/* Linear::solve(sol, rhs, tol_rel, tol_abs): MLMG solve, sol updated in place,
+ * Linear.H:131-147.  Like MLMG::solve it re-runs prepareForSolve (coefficient
+ * averaging and diagonals) on every call.  Convergence: ||b - A x||_inf <=
+ * max(tol_abs, tol_rel * max(||b||_inf, ||b - A x0||_inf)). */
+agb_status agb_solve(agb_solver s, double* sol, const double* rhs, double tol_rel, double tol_abs, int mem,
+                     agb_solve_report* report);
+/* Linear::apply(out, in), Linear.H:169-174 */
+agb_status agb_apply(agb_solver s, double* out, const double* in, int mem);
+
+/* Newton-step helpers (one Newton iteration = the linear-model solve):
+ *   BC::Operator::Elastic::Constant::Init, Constant.H:100-194
+ *   Newton::prepareForSolve RHS, Solver/Nonlocal/Newton.H:144-275
+ *   Newton::solve, Newton.H:279-358 (u += dsol)
+ *   stress = DW(grad u), Integrator/Base/Mechanics.H:210-236 (9 per node, row-major, AoS)
+ *   trac_hi[0] integral, Integrator/Base/Mechanics.H:391-431
+ * F0 (eigenstrain, 9 doubles per node, AoS row-major, Model/Solid/Affine) may be NULL. */
+agb_status agb_bc_init(agb_op op, double* rhs, int homogeneous, int mem);
+agb_status agb_newton_rhs(agb_op op, const double* F0, const double* u, const double* b, double* rhs, int mem);
+agb_status agb_newton_solve(agb_solver s, const double* F0, double* u, const double* b, double tol_rel,
+                            double tol_abs, int mem, agb_solve_report* report);
+agb_status agb_stress(agb_op op, const double* F0, const double* u, double* sigma9, int mem);
+agb_status agb_traction_xhi(agb_op op, const double* F0, const double* u, double trac[3], int mem);
+
+/* Timing hook used by the benchmark: runs `reps` launches of one internal
+ * stencil sweep (mode 0 apply, 1 residual, 2 Jacobi) at `level` in FP64
+ * (precision AGB_PREC_F64) or FP32 (AGB_PREC_MIXED) on the operator's resident
+ * buffers, and returns the mean device time of one launch in ms (CUDA events
+ * on the operator stream). */
+agb_status agb_op_time_sweep(agb_op op, int level, int precision, int mode, int reps, double* ms_per_launch);
+
+/* Pinned host memory (for callers that want asynchronous copies). */
+agb_status agb_host_alloc(size_t bytes, void** p);
+agb_status agb_host_free(void* p);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,67 @@
+"""Extract the reference's known-answer data for the elastic path into
+tests/golden/solid_kat.json.
+
+Run here (where the reference tree is mounted); the JSON travels with the
+repository.  Sources (paths relative to the alamo tree):
+  tests/Solid/input, tests/Solid/test                 4^3 cells, tensiontest
+                                                      uniaxial_stress, disp (0,1:0,0.01),
+                                                      tolerance 1e-4
+  tests/Solid/reference/linear-cubic.dat, affine-cubic.dat   trac_xhi_x vs time
+  tests/UniaxialTension/input, tests/UniaxialTension/test    analytic u_x, sigma_xx,
+                                                      tolerance 1e-8
+"""
+import json
+import os
+import sys
+
+REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "solid_kat.json")
+
+
+def load_dat(path):
+    with open(path) as f:
+        head = f.readline().split()
+        rows = [list(map(float, line.split())) for line in f if line.strip()]
+    return {h: [r[i] for r in rows] for i, h in enumerate(head)}
+
+
+def parse_bc(path):
+    """bc.constant.type.<region> / bc.constant.val.<region> lines of a reference input file."""
+    out = {}
+    for line in open(path):
+        line = line.split("#")[0].strip()
+        if not line.startswith("bc.constant."):
+            continue
+        key, val = [t.strip() for t in line.split("=", 1)]
+        kind, region = key.split(".")[2], key.split(".")[3]
+        toks = val.split()
+        out[("val." if kind == "val" else "") + region] = [float(t) for t in toks] if kind == "val" else toks
+    return out
+
+
+def main():
+    solid = os.path.join(REF, "tests", "Solid")
+    out = {
+        "source": "alamo tests/Solid/reference/*.dat and tests/UniaxialTension (analytic)",
+        "solid": {
+            "n_cells": [4, 4, 4], "prob_lo": [0, 0, 0], "prob_hi": [1, 1, 1],
+            "bc": {"type": "uniaxial_stress", "disp_of_t": [[0.0, 0.0], [1.0, 0.01]]},
+            "moduli": {"C11": 168.3, "C12": 1.221, "C44": 0.757},
+            "tolerance": 1e-4,
+            "linear-cubic": load_dat(os.path.join(solid, "reference", "linear-cubic.dat")),
+            "affine-cubic": load_dat(os.path.join(solid, "reference", "affine-cubic.dat")),
+            "affine_F0": [0.001, 0, 0, 0, 0.001, 0, 0, 0, 0.001],
+        },
+        "uniaxial_tension": {
+            "E": 210.0, "nu": 0.3, "disp": 0.1, "L": 16.0, "prob_lo": [-8, -8, -8], "prob_hi": [8, 8, 8],
+            "tolerance": 1e-8,
+            "bc_constant": parse_bc(os.path.join(REF, "tests", "UniaxialTension", "input")),
+        },
+    }
+    with open(OUT, "w") as f:
+        json.dump(out, f, indent=1)
+    print("wrote", OUT)
+
+
+if __name__ == "__main__":
+    main()
