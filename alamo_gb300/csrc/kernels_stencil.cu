@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdio>
+#include <cstdlib>
 
 #include "agb_internal.h"
 #include "stencil.cuh"
@@ -163,6 +164,65 @@ __global__ void __launch_bounds__(256) k_stencil_node(LevelDesc L, BCTable bc, G
 }
 
 // ---------------------------------------------------------------------------
+// boundary shell of a box with no periodic direction: one thread per boundary
+// node, enumerated plane k=0, plane k=n2, then the rings of the planes between
+// ---------------------------------------------------------------------------
+__host__ __device__ inline long long shell_count(const LevelDesc& L)
+{
+    const long long a = (long long)L.nn[0] * L.nn[1];
+    return 2 * a + (long long)(L.nn[2] - 2) * (2LL * L.nn[0] + 2LL * (L.nn[1] - 2));
+}
+
+__device__ __forceinline__ void shell_node(const LevelDesc& L, long long e, int& i, int& j, int& k)
+{
+    const long long a = (long long)L.nn[0] * L.nn[1];
+    if (e < 2 * a) {
+        k = e < a ? 0 : L.nn[2] - 1;
+        const long long r = e < a ? e : e - a;
+        j = (int)(r / L.nn[0]);
+        i = (int)(r % L.nn[0]);
+        return;
+    }
+    const long long e2 = e - 2 * a, pm = 2LL * L.nn[0] + 2LL * (L.nn[1] - 2);
+    k = 1 + (int)(e2 / pm);
+    const int r = (int)(e2 % pm);
+    if (r < 2 * L.nn[0]) {
+        j = r < L.nn[0] ? 0 : L.nn[1] - 1;
+        i = r < L.nn[0] ? r : r - L.nn[0];
+    } else {
+        const int r2 = r - 2 * L.nn[0];
+        j = 1 + r2 / 2;
+        i = (r2 & 1) ? L.nn[0] - 1 : 0;
+    }
+}
+
+template <typename T, int SYM, int MODE>
+__global__ void __launch_bounds__(256) k_stencil_shell(LevelDesc L, BCTable bc, Geo<T> g, const T* __restrict__ ddw,
+                                                       const T* __restrict__ x, const T* __restrict__ b,
+                                                       const T* __restrict__ dinv, T* __restrict__ out, T omega,
+                                                       void* norm_slot)
+{
+    const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    T nrm = 0;
+    if (e < shell_count(L)) {
+        int i, j, k;
+        shell_node(L, e, i, j, k);
+        const int pos[3] = {i, j, k};
+        int mn[3], mx[3];
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            mn[d] = pos[d] == 0;
+            mx[d] = pos[d] == L.n[d];
+        }
+        GlobalAcc<T> acc{x, ddw, L.S, make_nbr(L, i, j, k)};
+        T f[3];
+        boundary_row<T, SYM>(acc, g, bc, mn, mx, f);
+        epilogue<T, MODE>(f, x, b, dinv, out, L.S, acc.nb.base, omega, nrm);
+    }
+    if (MODE == MODE_RESID && norm_slot) block_max_to_slot<T>(nrm, norm_slot);
+}
+
+// ---------------------------------------------------------------------------
 // k-marching interior kernel
 // ---------------------------------------------------------------------------
 constexpr int MT_X = 32, MT_Y = 8, MT_Z = 16;   // tile and k-chunk
@@ -304,12 +364,26 @@ static inline dim3 node_grid(const LevelDesc& L, dim3 blk)
     return dim3((L.nn[0] + blk.x - 1) / blk.x, (L.nn[1] + blk.y - 1) / blk.y, (L.nn[2] + blk.z - 1) / blk.z);
 }
 
+// Smallest cell count per direction for which the interior goes to the
+// marching kernel (AGB_MARCH_MIN_CELLS overrides; used for tile studies).
+int march_min_cells()
+{
+    static int v = [] {
+        const char* s = getenv("AGB_MARCH_MIN_CELLS");
+        return s ? atoi(s) : 128;
+    }();
+    return v;
+}
+
 template <typename T, int SYM, int MODE>
 static void stencil_dispatch(cudaStream_t st, const LevelDesc& L, const BCTable& bc, bool uniform, const T* ddw,
                              const T* x, const T* b, const T* diag, T* out, T omega, void* norm_slot)
 {
     const Geo<T> g = make_geo<T>(L);
-    const bool big = !L.per[0] && !L.per[1] && !L.per[2] && L.n[0] >= 32 && L.n[1] >= 8 && L.n[2] >= 8;
+    // The marching kernel pays one exposed load round trip per plane, so it
+    // only wins once the box is large enough to fill every SM several times.
+    const bool big = !L.per[0] && !L.per[1] && !L.per[2] && L.n[0] >= march_min_cells() &&
+                     L.n[1] >= 16 && L.n[2] >= 16;
     if (big) {
         // interior by the marching kernel, boundary shell by the per-node kernel
         const size_t smem = sizeof(MarchSmem<T, SYM>);
@@ -317,9 +391,10 @@ static void stencil_dispatch(cudaStream_t st, const LevelDesc& L, const BCTable&
         dim3 grd((L.n[0] - 1 + MT_X - 1) / MT_X, (L.n[1] - 1 + MT_Y - 1) / MT_Y, (L.n[2] - 1 + MT_Z - 1) / MT_Z);
         k_stencil_march<T, SYM, MODE><<<grd, blk, smem, st>>>(L, g, uniform ? 1 : 0, ddw, x, b, diag, out, omega,
                                                                 norm_slot); count_launch();
-        dim3 b2(32, 4, 2);
-        k_stencil_node<T, SYM, MODE><<<node_grid(L, b2), b2, 0, st>>>(L, bc, g, uniform ? 1 : 0, ddw, x, b, diag,
-                                                                       out, omega, norm_slot, 1); count_launch();
+        const long long ns = shell_count(L);
+        k_stencil_shell<T, SYM, MODE><<<(unsigned)((ns + 255) / 256), 256, 0, st>>>(L, bc, g, ddw, x, b, diag, out,
+                                                                                    omega, norm_slot);
+        count_launch();
     } else {
         dim3 b2(32, 4, 2);
         if (L.nn[0] <= 16) b2 = dim3(8, 8, 4);

@@ -1,0 +1,403 @@
+#!/usr/bin/env python3
+"""Benchmark: time to solve the 257^3-node cubic polycrystal to 1e-8 FP64
+relative residual on one GB300, plus the dominant kernel's roofline.
+
+Workload (seeded, synthetic; no dataset): 256^3 cells on the unit cube, 64
+Voronoi grains with uniformly random orientations of cubic C11=1.68,
+C12=1.21, C44=0.75; TensionTest uniaxial_stress with u_x = 0.01 on +x.
+
+One step = one full solve from u = 0 through the C ABI (prepareForSolve +
+MLMG iterations), run as FP32 cycles inside FP64 iterative refinement.  The
+plain FP64 multigrid solve of the same system is timed once beside it.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`--impl reference` times the CPU restatement of the reference algorithm
+(oracle/, OpenMP on every host core) on a bounded sample of the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Solve s @257^3 nodes to 1e-8 FP64 residual, learned+FP32 vs plain; Fapply GB/s"
+WORKLOAD = ("257^3-node cubic Voronoi polycrystal (64 grains, C11/C12/C44 = 1.68/1.21/0.75), "
+            "uniaxial tension u_x=0.01, solve to 1e-8 relative FP64 residual")
+BYTES_PER_NODE = {"jacobi_f32_cubic": 132, "fapply_f32_cubic": 108, "jacobi_f64_cubic": 264,
+                  "fapply_f64_cubic": 216}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=256, help="cells per direction")
+    ap.add_argument("--grains", type=int, default=64)
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 solve")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--cycle", default="F", choices=["F", "V"])
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# process group (one replica per GPU; no collective on the data path)
+# ---------------------------------------------------------------------------
+class Dist:
+    def __init__(self):
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch
+            import torch.distributed as dist
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+            if backend == "nccl":
+                torch.cuda.set_device(self.local)
+            dist.init_process_group(backend)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v):
+        if not self.pg:
+            return v
+        import torch
+        dev = "cuda" if self.pg.get_backend() == "nccl" else "cpu"
+        t = torch.tensor([float(v)], dtype=torch.float64, device=dev)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v):
+        if not self.pg:
+            return v
+        import torch
+        dev = "cuda" if self.pg.get_backend() == "nccl" else "cpu"
+        t = torch.tensor([float(v)], dtype=torch.float64, device=dev)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.f = None
+
+    def start(self):
+        try:
+            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": []}
+        if not self.proc:
+            return out
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+                for k, nm in enumerate(names):
+                    if r[5 + k].strip().lower().startswith("active"):
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                pass
+        if sm:
+            out = {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                   "samples": len(sm)}
+        return out
+
+
+def measured_peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(p) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+# ---------------------------------------------------------------------------
+# workload
+# ---------------------------------------------------------------------------
+def workload(n, grains):
+    from alamo_gb300 import microstructure as M
+    from alamo_gb300.elastic import TensionTest
+    ddw, _, _ = M.voronoi_cubic(n, ngrains=grains, seed=20260)
+    bc = TensionTest("uniaxial_stress", disp=0.01)
+    return ddw, bc
+
+
+def run_ours(args, dist):
+    import numpy as np
+    import torch
+    from alamo_gb300 import Elastic, Linear, Newton
+
+    torch.cuda.set_device(dist.local)
+    n = args.n
+    nodes = (n + 1) ** 3
+    ddw_h, bc = workload(n, args.grains)
+    op = Elastic([n] * 3, None, "majorminor")
+    op.SetBC(bc)
+    ddw_d = torch.from_numpy(ddw_h).cuda()
+    op.SetModel(ddw_d)
+    b_h = op.BCInit(np.zeros(3 * nodes))
+    rhs_h = op.NewtonRHS(np.zeros(3 * nodes), b_h)
+    rhs_d = torch.from_numpy(rhs_h).cuda()
+    sol_d = torch.zeros(3 * nodes, dtype=torch.float64, device="cuda")
+    maxfmg = 100000000 if args.cycle == "F" else 0
+    mixed = Linear(op, precision=1, max_fmg_iter=maxfmg)
+
+    def one():
+        sol_d.zero_()
+        mixed.solve(sol_d, rhs_d, 1e-8, 0.0)
+        return mixed.report
+
+    for _ in range(args.warmup):
+        one()
+    torch.cuda.synchronize()
+    dist.barrier()
+    clocks = Clocks(dist.local)
+    clocks.start()
+    t0 = time.perf_counter()
+    reps = [one() for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    dist.barrier()
+    clk = clocks.stop()
+    dev_ms = [r.solve_ms for r in reps]
+    step_ms = dist.max(statistics.mean(dev_ms))
+    kernels = int(sum(r.kernels for r in reps))
+    last = reps[-1]
+    res = {
+        "step_ms": step_ms, "wall_ms": wall * 1000 / args.steps, "kernels": kernels, "clocks": clk,
+        "mixed": {"cycles": last.iterations, "refinements": last.refinements, "res0": last.res0,
+                  "res_final": last.res_final, "rhs_norm": last.rhs_norm, "nlevels": last.nlevels},
+    }
+
+    # roofline of the dominant kernel: the FP32 damped-Jacobi sweep on the finest level
+    ms_j32 = op.time_sweep(0, "f32", 2, 20)
+    ms_a32 = op.time_sweep(0, "f32", 0, 20)
+    ms_j64 = op.time_sweep(0, "f64", 2, 5)
+    res["kernels_ms"] = {"jacobi_f32": ms_j32, "fapply_f32": ms_a32, "jacobi_f64": ms_j64}
+    res["nodes"] = nodes
+
+    # plain FP64 multigrid of the same system, once
+    if not args.no_plain:
+        plain = Linear(op, precision=0, max_fmg_iter=maxfmg)
+        sol_d.zero_()
+        plain.solve(sol_d, rhs_d, 1e-8, 0.0)
+        pr = plain.report
+        res["plain"] = {"ms": pr.solve_ms, "iterations": pr.iterations, "res_final": pr.res_final,
+                        "status": pr.status}
+        plain.Clear()
+
+    # end to end through the reference-facing calls with host buffers:
+    # SetModel(host Matrix4 field) + Newton step (host u, host b) -> host u
+    if not args.no_e2e:
+        ddw_p = torch.from_numpy(ddw_h).pin_memory().numpy()
+        b_p = torch.from_numpy(b_h).pin_memory().numpy()
+        u_p = torch.zeros(3 * nodes, dtype=torch.float64).pin_memory().numpy()
+        newton = Newton(op, precision=1, max_fmg_iter=maxfmg)
+
+        def e2e_step():
+            u_p[:] = 0.0
+            op.SetModel(ddw_p)
+            newton.solve(u_p, b_p, None, 1e-8, 0.0)
+
+        e2e_step()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ke = 2
+        for _ in range(ke):
+            e2e_step()
+        e2e_s = dist.max((time.perf_counter() - t0) / ke)
+        res["e2e"] = {"value": e2e_s, "unit": "s",
+                      "h2d_bytes_per_step": int(ddw_p.nbytes + b_p.nbytes + u_p.nbytes),
+                      "d2h_bytes_per_step": int(u_p.nbytes)}
+        newton.Clear()
+        res["u_check"] = float(np.abs(u_p).max())
+    mixed.Clear()
+    op.close()
+    return res, ddw_h, bc
+
+
+def cpu_sample(n, ddw_h, bc, iterations):
+    """The oracle on every host core: prepareForSolve + one MLMG F-cycle
+    iteration at the full size, scaled to a full solve by `iterations`."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    g = O.make_grid([n] * 3, sym=O.MAJORMINOR, bc_type=bc.type, bc_val=bc.val)
+    N = O.nodes(g)
+    b = O.bc_init(g, np.zeros(3 * N))
+    rhs = O.newton_rhs(g, ddw_h, None, np.zeros(3 * N), b)
+    _, rep = O.solve(g, ddw_h, rhs, tol_rel=1e-8, tol_abs=0.0, params=O.default_params(max_iter=1))
+    cores = O.lib().orc_num_threads()
+    value = rep.t_setup + iterations * rep.t_iter
+    return {"value": value, "unit": "s", "cores": cores, "kind": "port",
+            "sample": "oracle/ CPU restatement, OpenMP %d threads: prepareForSolve + 1 F-cycle iteration at "
+                      "257^3 measured (%.2f s + %.2f s), scaled by the %d iterations the same FP64 algorithm "
+                      "needs" % (cores, rep.t_setup, rep.t_iter, iterations)}
+
+
+def main():
+    args = parse()
+    dist = Dist()
+    if args.impl == "reference":
+        return run_reference(args, dist)
+    res, ddw_h, bc = run_ours(args, dist)
+    peak, peak_kind = measured_peak_hbm()
+    nodes = res["nodes"]
+    ms = res["kernels_ms"]["jacobi_f32"]
+    achieved = BYTES_PER_NODE["jacobi_f32_cubic"] * nodes / (ms * 1e-3) / 1e9
+    traffic = profile_traffic().get("jacobi_f32_cubic_257", {}).get("dram_bytes_per_launch")
+    roof = {"kernel": "k_stencil_march<float,MajorMinor,Jacobi> + boundary shell (finest level)",
+            "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": peak_kind,
+            "bytes_per_launch": BYTES_PER_NODE["jacobi_f32_cubic"] * nodes, "ms_per_launch": ms}
+    extra = {
+        "fapply_f32_gbs": round(BYTES_PER_NODE["fapply_f32_cubic"] * nodes / (res["kernels_ms"]["fapply_f32"] * 1e-3)
+                                / 1e9, 1),
+        "jacobi_f64_gbs": round(BYTES_PER_NODE["jacobi_f64_cubic"] * nodes / (res["kernels_ms"]["jacobi_f64"] * 1e-3)
+                                / 1e9, 1),
+        "kernel_ms": res["kernels_ms"],
+        "mixed": res["mixed"],
+    }
+    if "plain" in res:
+        extra["plain_fp64_s"] = res["plain"]["ms"] / 1000.0
+        extra["plain_fp64_iterations"] = res["plain"]["iterations"]
+        extra["speedup_vs_plain_fp64"] = round(res["plain"]["ms"] / res["step_ms"], 2)
+    line = {
+        "metric": METRIC, "value": res["step_ms"] / 1000.0 / dist.world, "unit": "s", "n_gpus": dist.world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["step_ms"], "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic (seeded Voronoi polycrystal)",
+        "config": {"workload": WORKLOAD, "nodes": nodes, "method": "FP32 %s-cycles in FP64 iterative refinement"
+                   % args.cycle, "smoother": "2+2 Fsmooth (4+4 damped-Jacobi sweeps)",
+                   "l2": "inputs larger than L2 (modulus field 2.9 GB FP64 / 1.4 GB FP32)",
+                   "parallelism": "replicas" if dist.world > 1 else "single GPU"},
+        "roofline": roof,
+        "gpu_launches": res["kernels"],
+        "clocks": res["clocks"],
+    }
+    if "e2e" in res:
+        line["e2e"] = res["e2e"]
+    line.update(extra)
+    if dist.rank == 0 and not args.no_cpu:
+        iters = res.get("plain", {}).get("iterations") or 0
+        if iters:
+            line["cpu_baseline"] = cpu_sample(args.n, ddw_h, bc, iters)
+    dist.barrier()
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    dist.close()
+
+
+# ---------------------------------------------------------------------------
+# reference arm: the CPU restatement of the reference algorithm
+# ---------------------------------------------------------------------------
+ITERATIONS_FILE = os.path.join(ROOT, "profiles", "c2_iterations.json")
+
+
+def run_reference(args, dist):
+    if dist.rank != 0:
+        dist.close()
+        return
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    O.build()
+    n = args.n
+    try:
+        with open(ITERATIONS_FILE) as f:
+            iters = int(json.load(f)["plain_fp64_iterations"])
+    except Exception:
+        iters = None
+    ddw_h, bc = workload(n, args.grains)
+    g = O.make_grid([n] * 3, sym=O.MAJORMINOR, bc_type=bc.type, bc_val=bc.val)
+    N = O.nodes(g)
+    b = O.bc_init(g, np.zeros(3 * N))
+    rhs = O.newton_rhs(g, ddw_h, None, np.zeros(3 * N), b)
+    p1 = O.default_params(max_iter=1)
+
+    def step():
+        _, rep = O.solve(g, ddw_h, rhs, tol_rel=1e-8, tol_abs=0.0, params=p1)
+        return rep
+
+    for _ in range(args.warmup):
+        step()
+    vals, reps = [], []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r = step()
+        reps.append(r)
+        vals.append(r.t_setup + (iters or 1) * r.t_iter)
+    wall = (time.perf_counter() - t0) / args.steps
+    cores = O.lib().orc_num_threads()
+    v = statistics.mean(vals)
+    sample = ("oracle/ CPU restatement (FP64, OpenMP %d threads); each step = prepareForSolve + 1 F-cycle "
+              "iteration at 257^3 (mean %.2f s), scaled to a full solve by %s iterations"
+              % (cores, wall, iters if iters else "1 (iteration count unknown)"))
+    line = {"metric": METRIC, "value": v, "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": v * 1000.0, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Voronoi polycrystal)",
+            "config": {"workload": WORKLOAD, "nodes": N, "method": "MLMG F-cycles, FP64, CPU"},
+            "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": "s", "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    dist.close()
+
+
+if __name__ == "__main__":
+    main()

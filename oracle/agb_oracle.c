@@ -8,6 +8,7 @@
 #include "agb_oracle.h"
 
 #include <math.h>
+#include <omp.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -19,6 +20,8 @@
 enum { ST_LO = 0, ST_HI = 1, ST_CENTRAL = 2 }; /* Numeric::StencilType, Stencil.H:21 */
 
 int orc_ncoef(int sym) { return sym == ORC_ISO ? 2 : 21; }
+
+int orc_num_threads(void) { return omp_get_max_threads(); }
 
 long orc_nnodes(const orc_grid* g)
 {
@@ -970,6 +973,7 @@ int orc_solve(const orc_grid* g, const double* ddw, const orc_solver_params* p,
     mg_t m;
     memset(&m, 0, sizeof(m));
     m.p = p;
+    const double t0 = omp_get_wtime();
     m.L = orc_num_levels(g, p->max_coarsening_level);
     const int nc = orc_ncoef(g->sym);
     m.g[0] = *g;
@@ -999,6 +1003,8 @@ int orc_solve(const orc_grid* g, const double* ddw, const orc_solver_params* p,
     rep->nlevels = m.L;
     rep->status = 1;
     double norm = resnorm0;
+    const double t1 = omp_get_wtime();
+    rep->t_setup = t1 - t0;
     if (resnorm0 <= target) rep->status = 0;
     else {
         const long n3 = 3 * m.N[0];
@@ -1016,6 +1022,7 @@ int orc_solve(const orc_grid* g, const double* ddw, const orc_solver_params* p,
         }
     }
     rep->res_final = norm;
+    rep->t_iter = omp_get_wtime() - t1;
     for (int l = 0; l < m.L; l++) {
         if (l > 0) free(m.ddw[l]);
         free(m.diag[l]); free(m.cor[l]); free(m.res[l]); free(m.rescor[l]); free(m.hold[l]);

@@ -83,9 +83,12 @@ typedef struct {
     double res0;              /* ||b - A x0||_inf */
     double res_final;
     int nlevels;
+    double t_setup;           /* wall seconds: coefficient averaging, diagonals, first residual */
+    double t_iter;            /* wall seconds spent in the iterations */
 } orc_report;
 
 int    orc_ncoef(int sym);
+int    orc_num_threads(void);
 long   orc_nnodes(const orc_grid* g);
 void   orc_default_params(orc_solver_params* p);
 void   orc_coarsen(const orc_grid* fine, orc_grid* crse);

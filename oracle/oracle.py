@@ -62,6 +62,8 @@ class Report(ctypes.Structure):
         ("res0", ctypes.c_double),
         ("res_final", ctypes.c_double),
         ("nlevels", ctypes.c_int),
+        ("t_setup", ctypes.c_double),
+        ("t_iter", ctypes.c_double),
     ]
 
 
@@ -104,6 +106,7 @@ def lib():
         L.orc_default_params.argtypes = [P(Params)]
         L.orc_num_levels.argtypes = [g, ctypes.c_int]
         L.orc_num_levels.restype = ctypes.c_int
+        L.orc_num_threads.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -228,6 +231,8 @@ def stress(g, ddw, F0, u):
 
 def solve(g, ddw, b, x0=None, tol_rel=1e-8, tol_abs=0.0, params=None):
     x = np.zeros(3 * nodes(g)) if x0 is None else np.array(x0, dtype=np.float64, copy=True)
+    if x.shape != (3 * nodes(g),) or b.shape != (3 * nodes(g),) or ddw.size != ncoef(g) * nodes(g):
+        raise ValueError("field sizes do not match the grid")
     p = params or default_params()
     rep = Report()
     lib().orc_solve(ctypes.byref(g), _p(ddw), ctypes.byref(p), _p(x), _p(b), tol_rel, tol_abs,

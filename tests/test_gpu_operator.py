@@ -12,10 +12,11 @@ TOL64 = 1e-12
 TOL32 = 1e-5
 
 # (cells, dx, periodic): small boxes, a box large enough for the shared-memory
-# marching kernel (n0 >= 32, n1 >= 8, n2 >= 8), and periodic boxes
+# marching kernel and its boundary-shell kernel (n0 >= 128, n1, n2 >= 16), and
+# periodic boxes
 CASES = [
     ([8, 6, 10], [0.125, 0.2, 0.1], (0, 0, 0)),
-    ([40, 12, 10], [0.025, 0.09, 0.1], (0, 0, 0)),
+    ([128, 16, 18], [1 / 128, 0.06, 0.05], (0, 0, 0)),
     ([8, 6, 10], [0.125, 0.2, 0.1], (1, 0, 1)),
     ([6, 8, 4], [0.2, 0.1, 0.25], (1, 1, 1)),
 ]
