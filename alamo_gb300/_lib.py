@@ -116,6 +116,17 @@ def lib():
         "agb_op_time_sweep": (st, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]),
         "agb_host_alloc": (st, [ctypes.c_size_t, ctypes.POINTER(vp)]),
         "agb_host_free": (st, [vp]),
+        "agb_batch_create": (st, [ctypes.c_int, ip, dp, ip, ctypes.c_int, ctypes.POINTER(AgbSolverParams),
+                                  ctypes.POINTER(vp)]),
+        "agb_batch_destroy": (st, [vp]),
+        "agb_batch_set_bc": (st, [vp, ctypes.POINTER(AgbBC)]),
+        "agb_batch_set_model": (st, [vp, ctypes.c_int, vp, ctypes.c_int, ctypes.c_int]),
+        "agb_batch_set_eigenstrain": (st, [vp, dp]),
+        "agb_batch_solve": (st, [vp, ctypes.c_double, ctypes.c_double, ctypes.POINTER(AgbSolveReport),
+                                 ctypes.POINTER(AgbSolveReport)]),
+        "agb_batch_get_solution": (st, [vp, ctypes.c_int, vp, ctypes.c_int]),
+        "agb_batch_mean_stress": (st, [vp, dp]),
+        "agb_batch_tuning": (st, [vp, ctypes.c_int, ip]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

@@ -77,6 +77,7 @@ long long& launch_counter()
     static long long n = 0;
     return n;
 }
+void set_error(const char* msg) { g_err = msg ? msg : ""; }
 }  // namespace agb
 
 struct agb_op_s {
@@ -90,7 +91,7 @@ struct agb_op_s {
     std::vector<Level> lev;
     cudaStream_t st = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
-    double* d_slots = nullptr;   // 8 x 8 bytes of reduction slots
+    double* d_slots = nullptr;   // 16 x 8 bytes of reduction slots
     double* h_slots = nullptr;   // pinned mirror
     double* bottom_work = nullptr;
     int* d_ret = nullptr;
@@ -311,6 +312,20 @@ template <typename T> struct Engine {
         launch_stencil<T>(op->st, op->sym, MODE_RESID, v.L, op->bc, op->uniform, A::ddw(v), x, b, nullptr, r, (T)0,
                           slot);
     }
+    // The solve's fine-level residual and its max norm (into a zeroed slot).
+    // A fully periodic box is singular (rigid translations) and the operator
+    // is not conservative, so its left null vectors are constants only up to
+    // discretisation error: the solve projects the right-hand side and every
+    // fine residual (and, in the bottom solve, every Krylov residual and
+    // operator application) to zero mean per component, and so finds u with
+    // A u = b - c for a uniform body force c of the size of that error.
+    void fine_residual(const T* x, const T* b, T* r, void* slot)
+    {
+        Level& v = lv(0);
+        if (!v.L.singular()) return residual(0, x, b, r, slot);
+        residual(0, x, b, r, nullptr);
+        launch_remove_mean<T>(op->st, v.L, r, op->d_slots + 11, slot);
+    }
     void bottom()
     {
         Level& v = lv(bot());
@@ -384,7 +399,7 @@ void iter64_body(agb_solver s, int iter)
     E.cycle(iter);
     launch_axpy<double>(op->st, v0.L, 3, s->x64, v0.cor64, 1.0);
     cudaMemsetAsync(op->d_slots, 0, sizeof(double), op->st);
-    E.residual(0, s->x64, s->b64, v0.res64, op->d_slots);
+    E.fine_residual(s->x64, s->b64, v0.res64, op->d_slots);
     cudaMemcpyAsync(op->h_slots, op->d_slots, sizeof(double), cudaMemcpyDeviceToHost, op->st);
 }
 
@@ -397,7 +412,7 @@ void iter32_body(agb_solver s, int iter)
     E.cycle(iter);
     launch_axpy<float>(op->st, v0.L, 3, s->sol32, v0.cor32, 1.0f);
     cudaMemsetAsync(op->d_slots + 1, 0, sizeof(double), op->st);
-    E.residual(0, s->sol32, s->rhs32, v0.res32, op->d_slots + 1);
+    E.fine_residual(s->sol32, s->rhs32, v0.res32, op->d_slots + 1);
     cudaMemcpyAsync(op->h_slots + 1, op->d_slots + 1, sizeof(double), cudaMemcpyDeviceToHost, op->st);
 }
 
@@ -474,7 +489,7 @@ agb_status residual64(agb_solver s, double* norm)
     Engine<double> E{op, s->p};
     Level& v0 = op->lev[0];
     CK(cudaMemsetAsync(op->d_slots, 0, sizeof(double), op->st));
-    E.residual(0, s->x64, s->b64, v0.res64, op->d_slots);
+    E.fine_residual(s->x64, s->b64, v0.res64, op->d_slots);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(op->h_slots, op->d_slots, sizeof(double), cudaMemcpyDeviceToHost, op->st));
     double v;
@@ -684,12 +699,12 @@ agb_status agb_op_create(const int n_cells[3], const double dx[3], const int per
         if ((s = op->alloc(&lv.tmp64, n3)) != AGB_OK) return bail(s);
     }
     agb_status s;
-    if ((s = op->alloc(&op->d_slots, 8)) != AGB_OK) return bail(s);
+    if ((s = op->alloc(&op->d_slots, 16)) != AGB_OK) return bail(s);
     if ((s = op->alloc(&op->bottom_work, 8 * 3 * (size_t)op->lev.back().L.S)) != AGB_OK) return bail(s);
     if ((s = op->alloc(&op->d_ret, 4)) != AGB_OK) return bail(s);
     op->stage_bytes = 64u << 20;
     if ((s = op->alloc(&op->stage, op->stage_bytes)) != AGB_OK) return bail(s);
-    if (cudaMallocHost(&op->h_slots, 8 * sizeof(double)) != cudaSuccess)
+    if (cudaMallocHost(&op->h_slots, 16 * sizeof(double)) != cudaSuccess)
         return bail(fail(AGB_NOMEM, "cudaMallocHost failed"));
     if (cudaStreamSynchronize(op->st) != cudaSuccess) return bail(fail(AGB_CUDA, "stream sync failed"));
     *out = op;
@@ -945,8 +960,14 @@ static agb_status solve_resident(agb_solver s, double tol_rel, double tol_abs, a
     agb_op op = s->op;
     rep->nlevels = (int)op->lev.size();
     rep->refinements = 0;
-    if (s->p.precision == AGB_PREC_MIXED) return solve_mixed(s, tol_rel, tol_abs, rep);
-    return solve_plain(s, tol_rel, tol_abs, rep);
+    const LevelDesc& L0 = op->lev[0].L;
+    // fully periodic box: solve with the zero-mean part of b (Engine::fine_residual)
+    if (L0.singular()) launch_remove_mean<double>(op->st, L0, s->b64, op->d_slots + 8);
+    const agb_status st =
+        s->p.precision == AGB_PREC_MIXED ? solve_mixed(s, tol_rel, tol_abs, rep) : solve_plain(s, tol_rel, tol_abs, rep);
+    // and return the displacement modulo rigid translation: zero mean
+    if (L0.singular()) launch_remove_mean<double>(op->st, L0, s->x64, op->d_slots + 8);
+    return st;
 }
 
 agb_status agb_solve(agb_solver s, double* sol, const double* rhs, double tol_rel, double tol_abs, int mem,

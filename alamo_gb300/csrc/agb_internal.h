@@ -40,6 +40,9 @@ struct LevelDesc {
     long long S;     // component stride (elements), multiple of 64
     double dx[3];
 
+    // fully periodic: the operator is singular (rigid translations)
+    __host__ __device__ bool singular() const { return per[0] && per[1] && per[2]; }
+
     __host__ __device__ long long idx(int i, int j, int k) const
     {
         return (long long)i + (long long)P * ((long long)j + (long long)nn[1] * k);
@@ -56,7 +59,12 @@ inline LevelDesc make_level(const int n[3], const int per[3], const double dx[3]
         L.nn[d] = per[d] ? n[d] : n[d] + 1;
         L.dx[d] = dx[d];
     }
-    L.P = (L.nn[0] + 7) / 8 * 8;
+    // Row pitch: a multiple of 8 elements, and (for levels the marching
+    // kernels may serve: no periodic x) wide enough that their 36-element halo
+    // rows (starting at i = 32t) stay inside a row.
+    const int last_tile = n[0] >= 2 ? 32 * ((n[0] - 2) / 32) : 0;
+    const int need = (L.per[0] || L.nn[0] > last_tile + 36) ? L.nn[0] : last_tile + 36;
+    L.P = (need + 7) / 8 * 8;
     long long s = (long long)L.P * L.nn[1] * L.nn[2];
     L.S = (s + 63) / 64 * 64;
     return L;
@@ -66,8 +74,64 @@ inline LevelDesc make_level(const int n[3], const int per[3], const double dx[3]
 // this process; the benchmark reports kernels per solve from it.
 long long& launch_counter();
 inline void count_launch() { ++launch_counter(); }
+// Sets the thread-local message agb_last_error() returns.
+void set_error(const char* msg);
 
 enum StencilMode { MODE_APPLY = 0, MODE_RESID = 1, MODE_JACOBI = 2 };
+
+// ---------------------------------------------------------------------------
+// Batched solves: many independent boxes of different sizes per level.
+// Each problem's fields of one level live back to back in a level arena;
+// work is described by tiles (problem, block coordinates) that persistent
+// kernels stride over.
+// ---------------------------------------------------------------------------
+struct BProb {
+    LevelDesc L;
+    long long vo;     // element offset of this problem's 3-component vectors in the level arena
+    long long co;     // element offset of its moduli (ncoef planes)
+    long long wo;     // element offset of its bottom-solve work (8 x 3 planes, FP64)
+    int bottom;       // coarsest level of this problem
+    int pad;
+    double h1[3], i1[3], h2[3], hm[3];   // reciprocal grid factors (FP64)
+};
+
+struct BTile {
+    int prob;
+    short bx, by, bz;   // block coordinates inside the problem's level grid
+    short pad;
+};
+
+enum BatchVecOp { BV_ZERO = 0, BV_COPY = 1, BV_AXPY = 2, BV_SCALE_TO32 = 3, BV_ACC_FROM32 = 4 };
+
+template <typename T>
+void launch_batch_stencil(cudaStream_t st, int sym, int mode, int shape, int grid, const BProb* probs,
+                          const BTile* tiles, int ntiles, const int* active, const BCTable& bc, bool uniform,
+                          const T* ddw, const T* x, const T* b, const T* dinv, T* out, T omega, void* norm_slots);
+template <typename T>
+void launch_batch_transfer(cudaStream_t st, int restrict_not_interp, bool assign, int grid, const BProb* pf,
+                           const BProb* pc, const BTile* tiles, int ntiles, const int* active, const T* src, T* dst);
+void launch_batch_avg_ddw(cudaStream_t st, int grid, const BProb* pf, const BProb* pc, const BTile* tiles, int ntiles,
+                          const double* fine, double* crse, int ncoef);
+void launch_batch_diag(cudaStream_t st, int sym, int grid, const BProb* probs, const BTile* tiles, int ntiles,
+                       const BCTable& bc, const double* ddw, double* diag, double* dinv64, float* dinv32);
+void launch_batch_vec(cudaStream_t st, int op, int grid, const BProb* probs, const BTile* tiles, int ntiles,
+                      const int* active, void* y, const void* x, double a, const double* scale, int fp32);
+void launch_batch_bottom(cudaStream_t st, int sym, int fp32, const BProb* probs, const int* plist, int np,
+                         const int* active, const BCTable& bc, bool uniform, const double* ddw, const double* diag,
+                         void* cor, const void* res, double* work, int maxiter, double tol_rel, double tol_abs, int nub,
+                         int nuf, double omega);
+void launch_batch_rhs(cudaStream_t st, int sym, int grid, const BProb* probs, const BTile* tiles, int ntiles,
+                      const double* ddw, const double* F0, double* rhs);
+void launch_batch_mean_stress(cudaStream_t st, int sym, int grid, const BProb* probs, const BTile* tiles, int ntiles,
+                              const double* ddw, const double* F0, const double* u, double* sums);
+// per-problem component sums of y over the stored nodes into sums (3 per
+// problem, zeroed by the caller), or (subtract) y -= sums / count, with the
+// per-problem max |y| after it into norm_slots when given
+template <typename T>
+void launch_batch_mean3(cudaStream_t st, int grid, const BProb* probs, const BTile* tiles, int ntiles,
+                        const int* active, T* y, double* sums, int subtract, void* norm_slots = nullptr);
+int batch_shape_count();
+void batch_shape_dims(int shape, int dims[3]);
 
 // Launchers (kernels_*.cu).  All work is queued on `st`; none synchronizes.
 template <typename T>
@@ -104,6 +168,10 @@ template <typename TD, typename TS>
 void launch_export(cudaStream_t st, const LevelDesc& L, int ncomp, const TS* src, TD* dst, bool aos, int k0, int kc,
                    bool chunk);
 void launch_axpy_mixed(cudaStream_t st, const LevelDesc& L, int ncomp, double* y, const float* x, double a);
+// x -= per-component mean over the stored nodes (sums3: 3 doubles of scratch);
+// with norm_slot, also max |x| after the subtraction (atomic max into a zeroed slot)
+template <typename T>
+void launch_remove_mean(cudaStream_t st, const LevelDesc& L, T* x, double* sums3, void* norm_slot = nullptr);
 template <typename TD>
 void launch_recip(cudaStream_t st, const LevelDesc& L, int ncomp, const double* d, TD* r);
 void init_kernel_attributes();

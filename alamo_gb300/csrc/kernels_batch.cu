@@ -1,0 +1,834 @@
+// kernels_batch.cu -- batched solves of many independent boxes (periodic RVEs
+// of different sizes) with persistent tile kernels.
+//
+// A level arena holds every problem's fields of that level back to back
+// (BProb gives the offsets).  A tile list names (problem, block) pairs; each
+// kernel is launched with a grid sized to the GPU (a few CTAs per SM) and its
+// CTAs stride over the tile list, so one launch covers all problems of the
+// level whatever their sizes.  Problems already converged are skipped through
+// the `active` flags, so the same captured graph serves every iteration.
+//
+// Per-node arithmetic is the single-box arithmetic of stencil.cuh
+// (Operator/Elastic.cpp:141-292; transfers Operator.cpp:262-434).
+#include <cuda_runtime.h>
+
+#include "agb_internal.h"
+#include "stencil.cuh"
+
+namespace agb {
+
+static const int kShapes[5][3] = {{32, 4, 2}, {32, 8, 1}, {16, 8, 2}, {8, 8, 4}, {64, 4, 1}};
+int batch_shape_count() { return 5; }
+void batch_shape_dims(int shape, int dims[3])
+{
+    for (int d = 0; d < 3; d++) dims[d] = kShapes[shape][d];
+}
+
+template <typename T> __device__ __forceinline__ Geo<T> geo_of(const BProb& p)
+{
+    Geo<T> g;
+    for (int d = 0; d < 3; d++) {
+        g.h1[d] = (T)p.h1[d];
+        g.i1[d] = (T)p.i1[d];
+        g.h2[d] = (T)p.h2[d];
+        g.hm[d] = (T)p.hm[d];
+    }
+    return g;
+}
+
+struct BNbr {
+    long long base;
+    long long o[3][3];
+};
+
+__device__ __forceinline__ BNbr bnbr(const LevelDesc& L, int i, int j, int k)
+{
+    BNbr nb;
+    nb.base = L.idx(i, j, k);
+    const long long st[3] = {1, (long long)L.P, (long long)L.P * L.nn[1]};
+    const int pos[3] = {i, j, k};
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        nb.o[d][0] = -st[d];
+        nb.o[d][1] = 0;
+        nb.o[d][2] = st[d];
+        if (L.per[d]) {
+            if (pos[d] == 0) nb.o[d][0] = st[d] * (L.n[d] - 1);
+            if (pos[d] == L.n[d] - 1) nb.o[d][2] = -st[d] * (L.n[d] - 1);
+        }
+    }
+    return nb;
+}
+
+template <typename T> struct BAcc {
+    const T* __restrict__ x;
+    const T* __restrict__ c;
+    long long S;
+    BNbr nb;
+    __device__ __forceinline__ long long off(int di, int dj, int dk) const
+    {
+        return nb.base + nb.o[0][di + 1] + nb.o[1][dj + 1] + nb.o[2][dk + 1];
+    }
+    __device__ __forceinline__ T u(int p, int di, int dj, int dk) const { return __ldg(x + p * S + off(di, dj, dk)); }
+    __device__ __forceinline__ T C(int m, int di, int dj, int dk) const { return __ldg(c + m * S + off(di, dj, dk)); }
+};
+
+template <typename T> struct SlotMax;
+template <> struct SlotMax<double> {
+    static __device__ void put(void* s, int p, double v)
+    {
+        atomicMax((unsigned long long*)s + p, (unsigned long long)__double_as_longlong(v));
+    }
+};
+template <> struct SlotMax<float> {
+    static __device__ void put(void* s, int p, float v) { atomicMax((unsigned int*)s + 2 * p, __float_as_uint(v)); }
+};
+
+// block max of v over threads sharing the tile (all of the CTA) -> slot[prob]
+template <typename T> __device__ __forceinline__ void tile_max(T v, void* slots, int prob)
+{
+    __shared__ T red[32];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int o = 16; o > 0; o >>= 1) {
+        const T w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = (w > v || w != w) ? w : v;
+    }
+    __syncthreads();
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        v = lane < (int)(blockDim.x >> 5) ? red[lane] : (T)0;
+        for (int o = 16; o > 0; o >>= 1) {
+            const T w = __shfl_xor_sync(0xffffffffu, v, o);
+            v = (w > v || w != w) ? w : v;
+        }
+        if (lane == 0) SlotMax<T>::put(slots, prob, v);
+    }
+}
+
+// node of the tile handled by this thread (1D CTA of 256 threads)
+template <int BX, int BY, int BZ>
+__device__ __forceinline__ bool tile_node(const BTile& t, const LevelDesc& L, int& i, int& j, int& k)
+{
+    const int tid = threadIdx.x;
+    i = t.bx * BX + tid % BX;
+    j = t.by * BY + (tid / BX) % BY;
+    k = t.bz * BZ + tid / (BX * BY);
+    return i < L.nn[0] && j < L.nn[1] && k < L.nn[2];
+}
+
+template <typename T, int SYM, int MODE, int BX, int BY, int BZ>
+__global__ void __launch_bounds__(256) k_batch_stencil(const BProb* __restrict__ probs, const BTile* __restrict__ tiles,
+                                                       int ntiles, const int* __restrict__ active, BCTable bc,
+                                                       int uniform, const T* __restrict__ ddw,
+                                                       const T* __restrict__ x, const T* __restrict__ b,
+                                                       const T* __restrict__ dinv, T* __restrict__ out, T omega,
+                                                       void* norm_slots)
+{
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const BTile tl = tiles[t];
+        if (active && !active[tl.prob]) continue;   // uniform over the CTA
+        const BProb& P = probs[tl.prob];
+        const LevelDesc& L = P.L;
+        int i, j, k;
+        const bool ok = tile_node<BX, BY, BZ>(tl, L, i, j, k);
+        T nrm = 0;
+        if (ok) {
+            const Geo<T> g = geo_of<T>(P);
+            const T* xp = x + P.vo;
+            BAcc<T> acc{xp, ddw + P.co, L.S, bnbr(L, i, j, k)};
+            const int pos[3] = {i, j, k};
+            int mn[3], mx[3];
+            bool bnd = false;
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+                mn[d] = !L.per[d] && pos[d] == 0;
+                mx[d] = !L.per[d] && pos[d] == L.n[d];
+                bnd = bnd || mn[d] || mx[d];
+            }
+            T f[3];
+            if (bnd) boundary_row<T, SYM>(acc, g, bc, mn, mx, f);
+            else interior_row<T, SYM>(acc, g, uniform != 0, f);
+            const long long q = P.vo + acc.nb.base;
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                const long long o = q + c * L.S;
+                if (MODE == MODE_APPLY) out[o] = f[c];
+                else if (MODE == MODE_RESID) {
+                    const T r = b[o] - f[c];
+                    out[o] = r;
+                    const T a = fabs(r);
+                    nrm = (a > nrm || a != a) ? a : nrm;
+                } else {
+                    out[o] = x[o] + omega * ((b[o] - f[c]) * dinv[o]);
+                }
+            }
+        }
+        if (MODE == MODE_RESID && norm_slots) tile_max<T>(nrm, norm_slots, tl.prob);
+    }
+}
+
+// Full weighting (restriction) or trilinear prolongation between the levels of
+// every listed problem.  Tiles cover the destination level.
+template <typename T, class F>
+__device__ __forceinline__ T fw(const F& f, bool bI, bool bJ, bool bK)
+{
+    if (bI && bJ && bK) return f(0, 0, 0);
+    if (bJ && bK) return (T)0.25 * f(-1, 0, 0) + (T)0.5 * f(0, 0, 0) + (T)0.25 * f(1, 0, 0);
+    if (bK && bI) return (T)0.25 * f(0, -1, 0) + (T)0.5 * f(0, 0, 0) + (T)0.25 * f(0, 1, 0);
+    if (bI && bJ) return (T)0.25 * f(0, 0, -1) + (T)0.5 * f(0, 0, 0) + (T)0.25 * f(0, 0, 1);
+    if (bI)
+        return (f(0, -1, -1) + (T)2 * f(0, 0, -1) + f(0, 1, -1) + (T)2 * f(0, -1, 0) + (T)4 * f(0, 0, 0) +
+                (T)2 * f(0, 1, 0) + f(0, -1, 1) + (T)2 * f(0, 0, 1) + f(0, 1, 1)) * (T)(1.0 / 16.0);
+    if (bJ)
+        return (f(-1, 0, -1) + (T)2 * f(-1, 0, 0) + f(-1, 0, 1) + (T)2 * f(0, 0, -1) + (T)4 * f(0, 0, 0) +
+                (T)2 * f(0, 0, 1) + f(1, 0, -1) + (T)2 * f(1, 0, 0) + f(1, 0, 1)) * (T)(1.0 / 16.0);
+    if (bK)
+        return (f(-1, -1, 0) + (T)2 * f(0, -1, 0) + f(1, -1, 0) + (T)2 * f(-1, 0, 0) + (T)4 * f(0, 0, 0) +
+                (T)2 * f(1, 0, 0) + f(-1, 1, 0) + (T)2 * f(0, 1, 0) + f(1, 1, 0)) * (T)(1.0 / 16.0);
+    return (f(-1, -1, -1) + f(-1, -1, 1) + f(-1, 1, -1) + f(-1, 1, 1) + f(1, -1, -1) + f(1, -1, 1) + f(1, 1, -1) +
+            f(1, 1, 1)) * (T)(1.0 / 64.0) +
+           (f(0, -1, -1) + f(0, -1, 1) + f(0, 1, -1) + f(0, 1, 1) + f(-1, 0, -1) + f(1, 0, -1) + f(-1, 0, 1) +
+            f(1, 0, 1) + f(-1, -1, 0) + f(-1, 1, 0) + f(1, -1, 0) + f(1, 1, 0)) * (T)(1.0 / 32.0) +
+           (f(-1, 0, 0) + f(0, -1, 0) + f(0, 0, -1) + f(1, 0, 0) + f(0, 1, 0) + f(0, 0, 1)) * (T)(1.0 / 16.0) +
+           f(0, 0, 0) * (T)(1.0 / 8.0);
+}
+
+__device__ __forceinline__ int bwrap(int i, int n, int per)
+{
+    if (per) {
+        if (i < 0) return i + n;
+        if (i >= n) return i - n;
+    }
+    return i;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_batch_transfer(int restrict_not_interp, int assign,
+                                                        const BProb* __restrict__ pf, const BProb* __restrict__ pc,
+                                                        const BTile* __restrict__ tiles, int ntiles,
+                                                        const int* __restrict__ active, const T* __restrict__ src,
+                                                        T* __restrict__ dst)
+{
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const BTile tl = tiles[t];
+        if (active && !active[tl.prob]) continue;
+        const LevelDesc& Lf = pf[tl.prob].L;
+        const LevelDesc& Lc = pc[tl.prob].L;
+        const LevelDesc& Ld = restrict_not_interp ? Lc : Lf;
+        // tiles of batched transfers always use the 32x4x2 shape
+        int i, j, k;
+        if (!tile_node<32, 4, 2>(tl, Ld, i, j, k)) continue;
+        if (restrict_not_interp) {
+            const bool bI = !Lc.per[0] && (i == 0 || i == Lc.n[0]);
+            const bool bJ = !Lc.per[1] && (j == 0 || j == Lc.n[1]);
+            const bool bK = !Lc.per[2] && (k == 0 || k == Lc.n[2]);
+            const long long q = pc[tl.prob].vo + Lc.idx(i, j, k);
+            for (int c = 0; c < 3; c++) {
+                const T* s = src + pf[tl.prob].vo + c * Lf.S;
+                auto f = [&](int a, int b, int d) -> T {
+                    return __ldg(s + Lf.idx(bwrap(2 * i + a, Lf.n[0], Lf.per[0]), bwrap(2 * j + b, Lf.n[1], Lf.per[1]),
+                                            bwrap(2 * k + d, Lf.n[2], Lf.per[2])));
+                };
+                dst[q + c * Lc.S] = fw<T>(f, bI, bJ, bK);
+            }
+        } else {
+            const int I = i >> 1, J = j >> 1, K = k >> 1;
+            const int I1 = bwrap(I + 1, Lc.n[0], Lc.per[0]), J1 = bwrap(J + 1, Lc.n[1], Lc.per[1]),
+                      K1 = bwrap(K + 1, Lc.n[2], Lc.per[2]);
+            const bool ei = !(i & 1), ej = !(j & 1), ek = !(k & 1);
+            const long long q = pf[tl.prob].vo + Lf.idx(i, j, k);
+            for (int c = 0; c < 3; c++) {
+                const T* cs = src + pc[tl.prob].vo + c * Lc.S;
+                auto C = [&](int a, int b, int d) -> T { return __ldg(cs + Lc.idx(a ? I1 : I, b ? J1 : J, d ? K1 : K)); };
+                T v;
+                if (ei && ej && ek) v = C(0, 0, 0);
+                else if (ej && ek) v = (T)0.5 * (C(0, 0, 0) + C(1, 0, 0));
+                else if (ek && ei) v = (T)0.5 * (C(0, 0, 0) + C(0, 1, 0));
+                else if (ei && ej) v = (T)0.5 * (C(0, 0, 0) + C(0, 0, 1));
+                else if (ei) v = (T)0.25 * (C(0, 0, 0) + C(0, 1, 0) + C(0, 0, 1) + C(0, 1, 1));
+                else if (ej) v = (T)0.25 * (C(0, 0, 0) + C(0, 0, 1) + C(1, 0, 0) + C(1, 0, 1));
+                else if (ek) v = (T)0.25 * (C(0, 0, 0) + C(1, 0, 0) + C(0, 1, 0) + C(1, 1, 0));
+                else
+                    v = (T)0.125 * (C(0, 0, 0) + C(1, 0, 0) + C(0, 1, 0) + C(0, 0, 1) + C(0, 1, 1) + C(1, 0, 1) +
+                                    C(1, 1, 0) + C(1, 1, 1));
+                T* o = dst + q + c * Lf.S;
+                *o = assign ? v : (*o + v);
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_batch_avg_ddw(const BProb* __restrict__ pf, const BProb* __restrict__ pc,
+                                                       const BTile* __restrict__ tiles, int ntiles,
+                                                       const double* __restrict__ fine, double* __restrict__ crse,
+                                                       int ncoef)
+{
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const BTile tl = tiles[t];
+        const LevelDesc& Lf = pf[tl.prob].L;
+        const LevelDesc& Lc = pc[tl.prob].L;
+        int I, J, K;
+        if (!tile_node<32, 4, 2>(tl, Lc, I, J, K)) continue;
+        const bool bI = !Lc.per[0] && (I == 0 || I == Lc.n[0]);
+        const bool bJ = !Lc.per[1] && (J == 0 || J == Lc.n[1]);
+        const bool bK = !Lc.per[2] && (K == 0 || K == Lc.n[2]);
+        const long long q = pc[tl.prob].co + Lc.idx(I, J, K);
+        for (int m = 0; m < ncoef; m++) {
+            const double* s = fine + pf[tl.prob].co + m * Lf.S;
+            auto f = [&](int a, int b, int d) -> double {
+                return s[Lf.idx(bwrap(2 * I + a, Lf.n[0], Lf.per[0]), bwrap(2 * J + b, Lf.n[1], Lf.per[1]),
+                                bwrap(2 * K + d, Lf.n[2], Lf.per[2]))];
+            };
+            crse[q + m * Lc.S] = fw<double>(f, bI, bJ, bK);
+        }
+    }
+}
+
+template <int SYM>
+__global__ void __launch_bounds__(256) k_batch_diag(const BProb* __restrict__ probs, const BTile* __restrict__ tiles,
+                                                    int ntiles, BCTable bc, const double* __restrict__ ddw,
+                                                    double* __restrict__ diag, double* __restrict__ dinv64,
+                                                    float* __restrict__ dinv32)
+{
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const BTile tl = tiles[t];
+        const BProb& P = probs[tl.prob];
+        const LevelDesc& L = P.L;
+        int i, j, k;
+        if (!tile_node<32, 4, 2>(tl, L, i, j, k)) continue;
+        const int pos[3] = {i, j, k};
+        int mn[3], mx[3];
+        for (int d = 0; d < 3; d++) {
+            mn[d] = !L.per[d] && pos[d] == 0;
+            mx[d] = !L.per[d] && pos[d] == L.n[d];
+        }
+        const long long p = L.idx(i, j, k);
+        double c[NCoef<SYM>::value];
+        for (int m = 0; m < NCoef<SYM>::value; m++) c[m] = ddw[P.co + m * L.S + p];
+        for (int q = 0; q < 3; q++) {
+            const double d = diag_entry<double, SYM>(c, L, bc, mn, mx, q);
+            const long long o = P.vo + q * L.S + p;
+            diag[o] = d;
+            dinv64[o] = d != 0.0 ? 1.0 / d : 0.0;
+            if (dinv32) dinv32[o] = d != 0.0 ? (float)(1.0 / d) : 0.0f;
+        }
+    }
+}
+
+// Per-node vector operations over the listed problems (3 components).
+//   BV_ZERO        y = 0
+//   BV_COPY        y = x
+//   BV_AXPY        y += a x
+//   BV_SCALE_TO32  y(float) = x(double) / scale[prob]
+//   BV_ACC_FROM32  y(double) += x(float) * scale[prob]
+__global__ void __launch_bounds__(256) k_batch_vec(int op, const BProb* __restrict__ probs,
+                                                   const BTile* __restrict__ tiles, int ntiles,
+                                                   const int* __restrict__ active, void* y, const void* x, double a,
+                                                   const double* __restrict__ scale, int fp32)
+{
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const BTile tl = tiles[t];
+        if (active && !active[tl.prob]) continue;
+        const BProb& P = probs[tl.prob];
+        int i, j, k;
+        if (!tile_node<32, 4, 2>(tl, P.L, i, j, k)) continue;
+        const long long q0 = P.vo + P.L.idx(i, j, k);
+        for (int c = 0; c < 3; c++) {
+            const long long q = q0 + c * P.L.S;
+            if (op == BV_SCALE_TO32) {
+                ((float*)y)[q] = (float)(((const double*)x)[q] / scale[tl.prob]);
+            } else if (op == BV_ACC_FROM32) {
+                ((double*)y)[q] += (double)((const float*)x)[q] * scale[tl.prob];
+            } else if (fp32) {
+                float* yy = (float*)y;
+                const float* xx = (const float*)x;
+                if (op == BV_ZERO) yy[q] = 0.f;
+                else if (op == BV_COPY) yy[q] = xx[q];
+                else yy[q] += (float)a * xx[q];
+            } else {
+                double* yy = (double*)y;
+                const double* xx = (const double*)x;
+                if (op == BV_ZERO) yy[q] = 0.0;
+                else if (op == BV_COPY) yy[q] = xx[q];
+                else yy[q] += a * xx[q];
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// bottom solves: one CTA per problem (BiCGStab on the diagonally scaled
+// system + smoothing, as the single-box k_bottom).  On a fully periodic box
+// the Krylov residual and every operator application are projected to zero
+// mean per component (the box is singular: rigid translations).
+// ---------------------------------------------------------------------------
+constexpr int BB_THREADS = 256;
+
+__device__ __forceinline__ double bsum(double v, double* red)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double t = threadIdx.x < (BB_THREADS / 32) ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (threadIdx.x == 0) red[32] = t;
+    }
+    __syncthreads();
+    return red[32];
+}
+
+__device__ __forceinline__ double bmax(double v, double* red)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) {
+        const double w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = (w > v || w != w) ? w : v;
+    }
+    __syncthreads();
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double t = threadIdx.x < (BB_THREADS / 32) ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) {
+            const double w = __shfl_xor_sync(0xffffffffu, t, o);
+            t = (w > t || w != w) ? w : t;
+        }
+        if (threadIdx.x == 0) red[32] = t;
+    }
+    __syncthreads();
+    return red[32];
+}
+
+template <int SYM>
+__device__ void bapply(const BProb& P, const BCTable& bc, int uniform, const double* ddw, const double* x, double* y)
+{
+    const LevelDesc& L = P.L;
+    const Geo<double> g = geo_of<double>(P);
+    const long long cnt = L.count();
+    for (long long e = threadIdx.x; e < cnt; e += blockDim.x) {
+        const int i = (int)(e % L.nn[0]), j = (int)((e / L.nn[0]) % L.nn[1]),
+                  k = (int)(e / ((long long)L.nn[0] * L.nn[1]));
+        BAcc<double> acc{x, ddw, L.S, bnbr(L, i, j, k)};
+        const int pos[3] = {i, j, k};
+        int mn[3], mx[3];
+        bool bnd = false;
+        for (int d = 0; d < 3; d++) {
+            mn[d] = !L.per[d] && pos[d] == 0;
+            mx[d] = !L.per[d] && pos[d] == L.n[d];
+            bnd = bnd || mn[d] || mx[d];
+        }
+        double f[3];
+        if (bnd) boundary_row<double, SYM>(acc, g, bc, mn, mx, f);
+        else interior_row<double, SYM>(acc, g, uniform != 0, f);
+        for (int c = 0; c < 3; c++) y[c * L.S + acc.nb.base] = f[c];
+    }
+}
+
+__device__ void bmean3(const LevelDesc& L, const double* v, double* red, double m[3])
+{
+    const long long cnt = L.count();
+    double s0 = 0, s1 = 0, s2 = 0;
+    for (long long e = threadIdx.x; e < cnt; e += blockDim.x) {
+        const long long q = L.idx((int)(e % L.nn[0]), (int)((e / L.nn[0]) % L.nn[1]),
+                                  (int)(e / ((long long)L.nn[0] * L.nn[1])));
+        s0 += v[q];
+        s1 += v[L.S + q];
+        s2 += v[2 * L.S + q];
+    }
+    m[0] = bsum(s0, red) / (double)cnt;
+    m[1] = bsum(s1, red) / (double)cnt;
+    m[2] = bsum(s2, red) / (double)cnt;
+}
+
+#define BFOR(q)                                                                                        \
+    for (long long e_ = threadIdx.x; e_ < cnt; e_ += blockDim.x)                                       \
+        for (int c_ = 0, i_ = (int)(e_ % L.nn[0]), j_ = (int)((e_ / L.nn[0]) % L.nn[1]),                \
+                 k_ = (int)(e_ / ((long long)L.nn[0] * L.nn[1]));                                      \
+             c_ < 3; c_++)                                                                             \
+            for (long long q = c_ * L.S + L.idx(i_, j_, k_), once_ = 0; once_ < 1; once_++)
+
+template <typename T, int SYM>
+__global__ void __launch_bounds__(BB_THREADS) k_batch_bottom(const BProb* __restrict__ probs, const int* __restrict__ plist,
+                                                            const int* __restrict__ active, BCTable bc, int uniform,
+                                                            const double* __restrict__ ddw_all,
+                                                            const double* __restrict__ diag_all, T* __restrict__ cor_all,
+                                                            const T* __restrict__ res_all, double* __restrict__ work_all,
+                                                            int maxiter, double eps_rel, double eps_abs, int nub, int nuf,
+                                                            double omega)
+{
+    __shared__ double red[33];
+    const int pid = plist[blockIdx.x];
+    if (active && !active[pid]) return;
+    const BProb& P = probs[pid];
+    const LevelDesc& L = P.L;
+    const long long n3 = 3 * L.S, cnt = L.count();
+    const double* ddw = ddw_all + P.co;
+    const double* diag = diag_all + P.vo;
+    T* cor = cor_all + P.vo;
+    const T* res = res_all + P.vo;
+    double* w = work_all + P.wo;
+    double *r = w, *rh = w + n3, *p = w + 2 * n3, *v = w + 3 * n3, *s = w + 4 * n3, *t = w + 5 * n3, *sol = w + 6 * n3,
+           *b = w + 7 * n3;
+    BFOR(q)
+    {
+        b[q] = (double)res[q];
+        sol[q] = 0.0;
+    }
+    __syncthreads();
+    const bool sing = L.singular();
+    double mb[3] = {0, 0, 0};
+    if (sing) bmean3(L, b, red, mb);
+    double lm = 0;
+    BFOR(q)
+    {
+        r[q] = (b[q] - mb[c_]) / diag[q];
+        rh[q] = r[q];
+        const double a = fabs(r[q]);
+        lm = (a > lm || a != a) ? a : lm;
+    }
+    double rnorm = bmax(lm, red);
+    const double rnorm0 = rnorm;
+    int ret = 0;
+    double rho_1 = 0, alpha = 0, om = 0;
+    if (!(rnorm0 == 0 || rnorm0 < eps_abs)) {
+        for (int iter = 1; iter <= maxiter; iter++) {
+            double acc = 0;
+            BFOR(q) acc += rh[q] * r[q];
+            const double rho = bsum(acc, red);
+            if (rho == 0) { ret = 1; break; }
+            if (iter == 1) {
+                BFOR(q) p[q] = r[q];
+            } else {
+                const double beta = (rho / rho_1) * (alpha / om);
+                BFOR(q) p[q] = r[q] + beta * (p[q] - om * v[q]);
+            }
+            __syncthreads();
+            bapply<SYM>(P, bc, uniform, ddw, p, v);
+            __syncthreads();
+            double mv[3] = {0, 0, 0};
+            if (sing) bmean3(L, v, red, mv);
+            acc = 0;
+            BFOR(q)
+            {
+                v[q] = (v[q] - mv[c_]) / diag[q];
+                acc += rh[q] * v[q];
+            }
+            const double rhTv = bsum(acc, red);
+            if (rhTv != 0) alpha = rho / rhTv;
+            else { ret = 2; break; }
+            lm = 0;
+            BFOR(q)
+            {
+                sol[q] += alpha * p[q];
+                s[q] = r[q] - alpha * v[q];
+                const double a = fabs(s[q]);
+                lm = (a > lm || a != a) ? a : lm;
+            }
+            rnorm = bmax(lm, red);
+            if (rnorm < eps_rel * rnorm0 || rnorm < eps_abs) break;
+            bapply<SYM>(P, bc, uniform, ddw, s, t);
+            __syncthreads();
+            double mt[3] = {0, 0, 0};
+            if (sing) bmean3(L, t, red, mt);
+            double tt = 0, ts = 0;
+            BFOR(q)
+            {
+                t[q] = (t[q] - mt[c_]) / diag[q];
+                tt += t[q] * t[q];
+                ts += t[q] * s[q];
+            }
+            tt = bsum(tt, red);
+            ts = bsum(ts, red);
+            if (tt != 0) om = ts / tt;
+            else { ret = 3; break; }
+            lm = 0;
+            BFOR(q)
+            {
+                sol[q] += om * s[q];
+                r[q] = s[q] - om * t[q];
+                const double a = fabs(r[q]);
+                lm = (a > lm || a != a) ? a : lm;
+            }
+            rnorm = bmax(lm, red);
+            if (rnorm < eps_rel * rnorm0 || rnorm < eps_abs) break;
+            if (om == 0) { ret = 4; break; }
+            rho_1 = rho;
+        }
+        if (ret == 0 && rnorm > eps_rel * rnorm0 && rnorm > eps_abs) ret = 8;
+        if (ret != 0) {
+            BFOR(q) sol[q] = 0.0;
+        }
+    }
+    __syncthreads();
+    const int nsm = 2 * ((ret == 0) ? nub : nuf);
+    for (int sw = 0; sw < nsm; sw++) {
+        bapply<SYM>(P, bc, uniform, ddw, sol, t);
+        __syncthreads();
+        BFOR(q)
+        {
+            const double Rx = t[q] - sol[q] * diag[q];
+            s[q] = (1. - omega) * sol[q] + omega * (b[q] - Rx) / diag[q];
+        }
+        __syncthreads();
+        BFOR(q) sol[q] = s[q];
+        __syncthreads();
+    }
+    BFOR(q) cor[q] = (T)sol[q];
+}
+
+// rhs = -div(C : (0 - F0)) with a uniform eigenstrain F0 per problem: the
+// Newton right-hand side at u = 0 of an affine model (Newton.H:199-231,
+// Model/Solid/Affine/Isotropic.H:42-45) on a fully periodic box.
+template <int SYM>
+__global__ void __launch_bounds__(256) k_batch_rhs(const BProb* __restrict__ probs, const BTile* __restrict__ tiles,
+                                                   int ntiles, const double* __restrict__ ddw,
+                                                   const double* __restrict__ F0, double* __restrict__ rhs)
+{
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const BTile tl = tiles[t];
+        const BProb& P = probs[tl.prob];
+        const LevelDesc& L = P.L;
+        int i, j, k;
+        if (!tile_node<32, 4, 2>(tl, L, i, j, k)) continue;
+        const BNbr nb = bnbr(L, i, j, k);
+        double E[3][3];
+        for (int a = 0; a < 3; a++)
+            for (int c = 0; c < 3; c++) E[a][c] = 0.0 - F0[tl.prob * 9 + a * 3 + c];
+        double ret[3] = {0, 0, 0};
+        for (int d = 0; d < 3; d++) {
+            double cpv[NCoef<SYM>::value], cmv[NCoef<SYM>::value], Dp[3][3], Dm[3][3];
+            for (int m = 0; m < NCoef<SYM>::value; m++) {
+                cpv[m] = ddw[P.co + m * L.S + nb.base + nb.o[d][2]];
+                cmv[m] = ddw[P.co + m * L.S + nb.base + nb.o[d][0]];
+            }
+            c_mul_mat<double, SYM>(cpv, E, Dp);
+            c_mul_mat<double, SYM>(cmv, E, Dm);
+            for (int r = 0; r < 3; r++) ret[r] += (Dp[r][d] - Dm[r][d]) / 2. / L.dx[d];
+        }
+        for (int r = 0; r < 3; r++) rhs[P.vo + r * L.S + nb.base] = 0.0 - ret[r];
+    }
+}
+
+// Per-problem sums of sigma = C : (grad u - F0) over the stored nodes
+// (central differences; fully periodic boxes), for the homogenized stress.
+template <int SYM>
+__global__ void __launch_bounds__(256) k_batch_mean_stress(const BProb* __restrict__ probs,
+                                                           const BTile* __restrict__ tiles, int ntiles,
+                                                           const double* __restrict__ ddw,
+                                                           const double* __restrict__ F0,
+                                                           const double* __restrict__ u, double* __restrict__ sums)
+{
+    __shared__ double red[9][8];
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const BTile tl = tiles[t];
+        const BProb& P = probs[tl.prob];
+        const LevelDesc& L = P.L;
+        int i, j, k;
+        double S[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        if (tile_node<32, 4, 2>(tl, L, i, j, k)) {
+            const BNbr nb = bnbr(L, i, j, k);
+            double G[3][3], c[NCoef<SYM>::value];
+            for (int p = 0; p < 3; p++)
+                for (int d = 0; d < 3; d++)
+                    G[p][d] = (u[P.vo + p * L.S + nb.base + nb.o[d][2]] - u[P.vo + p * L.S + nb.base + nb.o[d][0]]) *
+                                  0.5 / L.dx[d] -
+                              F0[tl.prob * 9 + p * 3 + d];
+            for (int m = 0; m < NCoef<SYM>::value; m++) c[m] = ddw[P.co + m * L.S + nb.base];
+            c_mul_mat<double, SYM>(c, G, S);
+        }
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        for (int a = 0; a < 9; a++) {
+            double v = S[a / 3][a % 3];
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0) red[a][warp] = v;
+        }
+        __syncthreads();
+        if (threadIdx.x < 9) {
+            double v = 0;
+            for (int w = 0; w < 8; w++) v += red[threadIdx.x][w];
+            atomicAdd(&sums[tl.prob * 9 + threadIdx.x], v);
+        }
+        __syncthreads();
+    }
+}
+
+// per-problem component sums over the stored nodes (sums[prob*3 + c]); with
+// `subtract`, y -= sums/count instead
+template <typename T>
+__global__ void __launch_bounds__(256) k_batch_mean3(const BProb* __restrict__ probs, const BTile* __restrict__ tiles,
+                                                     int ntiles, const int* __restrict__ active, T* __restrict__ y,
+                                                     double* __restrict__ sums, int subtract, void* norm_slots)
+{
+    __shared__ double red[3][8];
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const BTile tl = tiles[t];
+        if (active && !active[tl.prob]) continue;   // uniform over the CTA
+        const BProb& P = probs[tl.prob];
+        int i, j, k;
+        const bool ok = tile_node<32, 4, 2>(tl, P.L, i, j, k);
+        const long long q = ok ? P.vo + P.L.idx(i, j, k) : 0;
+        if (subtract) {
+            T m = 0;
+            if (ok) {
+                const double cnt = (double)P.L.count();
+                for (int c = 0; c < 3; c++) {
+                    const T v = (T)((double)y[q + c * P.L.S] - sums[tl.prob * 3 + c] / cnt);
+                    y[q + c * P.L.S] = v;
+                    const T a = fabs(v);
+                    m = (a > m || a != a) ? a : m;
+                }
+            }
+            if (norm_slots) tile_max<T>(m, norm_slots, tl.prob);
+            continue;
+        }
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        for (int c = 0; c < 3; c++) {
+            double v = ok ? (double)y[q + c * P.L.S] : 0.0;
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0) red[c][warp] = v;
+        }
+        __syncthreads();
+        if (threadIdx.x < 3) {
+            double v = 0;
+            for (int w = 0; w < 8; w++) v += red[threadIdx.x][w];
+            atomicAdd(&sums[tl.prob * 3 + threadIdx.x], v);
+        }
+        __syncthreads();
+    }
+}
+
+template <typename T>
+void launch_batch_mean3(cudaStream_t st, int grid, const BProb* probs, const BTile* tiles, int ntiles,
+                        const int* active, T* y, double* sums, int subtract, void* norm_slots)
+{
+    k_batch_mean3<T><<<grid, 256, 0, st>>>(probs, tiles, ntiles, active, y, sums, subtract, norm_slots);
+    count_launch();
+}
+template void launch_batch_mean3<double>(cudaStream_t, int, const BProb*, const BTile*, int, const int*, double*,
+                                         double*, int, void*);
+template void launch_batch_mean3<float>(cudaStream_t, int, const BProb*, const BTile*, int, const int*, float*,
+                                        double*, int, void*);
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+template <typename T, int SYM, int MODE>
+static void bst_shape(cudaStream_t st, int shape, int grid, const BProb* probs, const BTile* tiles, int ntiles,
+                      const int* active, const BCTable& bc, bool uniform, const T* ddw, const T* x, const T* b,
+                      const T* dinv, T* out, T omega, void* norm)
+{
+#define L_(BX, BY, BZ)                                                                                      \
+    k_batch_stencil<T, SYM, MODE, BX, BY, BZ><<<grid, 256, 0, st>>>(probs, tiles, ntiles, active, bc, uniform ? 1 : 0, \
+                                                                     ddw, x, b, dinv, out, omega, norm)
+    switch (shape) {
+    case 0: L_(32, 4, 2); break;
+    case 1: L_(32, 8, 1); break;
+    case 2: L_(16, 8, 2); break;
+    case 3: L_(8, 8, 4); break;
+    default: L_(64, 4, 1); break;
+    }
+#undef L_
+    count_launch();
+}
+
+template <typename T>
+void launch_batch_stencil(cudaStream_t st, int sym, int mode, int shape, int grid, const BProb* probs,
+                          const BTile* tiles, int ntiles, const int* active, const BCTable& bc, bool uniform,
+                          const T* ddw, const T* x, const T* b, const T* dinv, T* out, T omega, void* norm_slots)
+{
+#define D_(S, M) bst_shape<T, S, M>(st, shape, grid, probs, tiles, ntiles, active, bc, uniform, ddw, x, b, dinv, out, omega, norm_slots)
+    if (sym == SYM_ISO) {
+        if (mode == MODE_APPLY) D_(SYM_ISO, MODE_APPLY);
+        else if (mode == MODE_RESID) D_(SYM_ISO, MODE_RESID);
+        else D_(SYM_ISO, MODE_JACOBI);
+    } else {
+        if (mode == MODE_APPLY) D_(SYM_MM, MODE_APPLY);
+        else if (mode == MODE_RESID) D_(SYM_MM, MODE_RESID);
+        else D_(SYM_MM, MODE_JACOBI);
+    }
+#undef D_
+}
+
+template <typename T>
+void launch_batch_transfer(cudaStream_t st, int restrict_not_interp, bool assign, int grid, const BProb* pf,
+                           const BProb* pc, const BTile* tiles, int ntiles, const int* active, const T* src, T* dst)
+{
+    k_batch_transfer<T><<<grid, 256, 0, st>>>(restrict_not_interp, assign ? 1 : 0, pf, pc, tiles, ntiles, active, src,
+                                              dst);
+    count_launch();
+}
+
+void launch_batch_avg_ddw(cudaStream_t st, int grid, const BProb* pf, const BProb* pc, const BTile* tiles, int ntiles,
+                          const double* fine, double* crse, int ncoef)
+{
+    k_batch_avg_ddw<<<grid, 256, 0, st>>>(pf, pc, tiles, ntiles, fine, crse, ncoef);
+    count_launch();
+}
+
+void launch_batch_diag(cudaStream_t st, int sym, int grid, const BProb* probs, const BTile* tiles, int ntiles,
+                       const BCTable& bc, const double* ddw, double* diag, double* dinv64, float* dinv32)
+{
+    if (sym == SYM_ISO) k_batch_diag<SYM_ISO><<<grid, 256, 0, st>>>(probs, tiles, ntiles, bc, ddw, diag, dinv64, dinv32);
+    else k_batch_diag<SYM_MM><<<grid, 256, 0, st>>>(probs, tiles, ntiles, bc, ddw, diag, dinv64, dinv32);
+    count_launch();
+}
+
+void launch_batch_vec(cudaStream_t st, int op, int grid, const BProb* probs, const BTile* tiles, int ntiles,
+                      const int* active, void* y, const void* x, double a, const double* scale, int fp32)
+{
+    k_batch_vec<<<grid, 256, 0, st>>>(op, probs, tiles, ntiles, active, y, x, a, scale, fp32);
+    count_launch();
+}
+
+void launch_batch_bottom(cudaStream_t st, int sym, int fp32, const BProb* probs, const int* plist, int np,
+                         const int* active, const BCTable& bc, bool uniform, const double* ddw, const double* diag,
+                         void* cor, const void* res, double* work, int maxiter, double tol_rel, double tol_abs, int nub,
+                         int nuf, double omega)
+{
+    if (np <= 0) return;
+#define B_(T, S)                                                                                                     \
+    k_batch_bottom<T, S><<<np, BB_THREADS, 0, st>>>(probs, plist, active, bc, uniform ? 1 : 0, ddw, diag, (T*)cor,     \
+                                                    (const T*)res, work, maxiter, tol_rel, tol_abs, nub, nuf, omega)
+    if (fp32) {
+        if (sym == SYM_ISO) B_(float, SYM_ISO);
+        else B_(float, SYM_MM);
+    } else {
+        if (sym == SYM_ISO) B_(double, SYM_ISO);
+        else B_(double, SYM_MM);
+    }
+#undef B_
+    count_launch();
+}
+
+void launch_batch_rhs(cudaStream_t st, int sym, int grid, const BProb* probs, const BTile* tiles, int ntiles,
+                      const double* ddw, const double* F0, double* rhs)
+{
+    if (sym == SYM_ISO) k_batch_rhs<SYM_ISO><<<grid, 256, 0, st>>>(probs, tiles, ntiles, ddw, F0, rhs);
+    else k_batch_rhs<SYM_MM><<<grid, 256, 0, st>>>(probs, tiles, ntiles, ddw, F0, rhs);
+    count_launch();
+}
+
+void launch_batch_mean_stress(cudaStream_t st, int sym, int grid, const BProb* probs, const BTile* tiles, int ntiles,
+                              const double* ddw, const double* F0, const double* u, double* sums)
+{
+    if (sym == SYM_ISO) k_batch_mean_stress<SYM_ISO><<<grid, 256, 0, st>>>(probs, tiles, ntiles, ddw, F0, u, sums);
+    else k_batch_mean_stress<SYM_MM><<<grid, 256, 0, st>>>(probs, tiles, ntiles, ddw, F0, u, sums);
+    count_launch();
+}
+
+template void launch_batch_stencil<double>(cudaStream_t, int, int, int, int, const BProb*, const BTile*, int,
+                                           const int*, const BCTable&, bool, const double*, const double*,
+                                           const double*, const double*, double*, double, void*);
+template void launch_batch_stencil<float>(cudaStream_t, int, int, int, int, const BProb*, const BTile*, int,
+                                          const int*, const BCTable&, bool, const float*, const float*, const float*,
+                                          const float*, float*, float, void*);
+template void launch_batch_transfer<double>(cudaStream_t, int, bool, int, const BProb*, const BProb*, const BTile*,
+                                            int, const int*, const double*, double*);
+template void launch_batch_transfer<float>(cudaStream_t, int, bool, int, const BProb*, const BProb*, const BTile*, int,
+                                           const int*, const float*, float*);
+
+}  // namespace agb

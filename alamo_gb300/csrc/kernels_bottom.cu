@@ -7,6 +7,10 @@
 //   a failed solve (anything but a clean convergence) zeroes the correction;
 //   then `bottom_smooth` (after success) or `final_smooth` (after failure)
 //   Fsmooth calls of 2 damped-Jacobi sweeps each.
+// On a fully periodic box (singular: rigid translations) the Krylov residual
+// and every operator application are projected to zero mean per component
+// before the diagonal scaling, so that BiCGStab works on a consistent system;
+// the smoothing uses the right-hand side as given.
 // Every loop is bounded by maxiter / the smoothing counts; there is no
 // spin-wait.  The return code lands in ret_slot: 0 converged, 1-4 breakdown,
 // 8 not converged in maxiter.
@@ -110,6 +114,24 @@ __device__ void cta_apply(const LevelDesc& L, const BCTable& bc, const Geo<doubl
     }
 }
 
+// per-component means over the level's nodes (every stored node is unique on
+// a fully periodic level)
+__device__ void cta_mean3(const LevelDesc& L, const double* v, double* red, double m[3])
+{
+    const long long cnt = L.count();
+    double s0 = 0, s1 = 0, s2 = 0;
+    for (long long e = threadIdx.x; e < cnt; e += blockDim.x) {
+        const long long q = L.idx((int)(e % L.nn[0]), (int)((e / L.nn[0]) % L.nn[1]),
+                                  (int)(e / ((long long)L.nn[0] * L.nn[1])));
+        s0 += v[q];
+        s1 += v[L.S + q];
+        s2 += v[2 * L.S + q];
+    }
+    m[0] = blk_sum(s0, red) / (double)cnt;
+    m[1] = blk_sum(s1, red) / (double)cnt;
+    m[2] = blk_sum(s2, red) / (double)cnt;
+}
+
 #define FOR_NODES(q)                                                                                     \
     for (long long e_ = threadIdx.x; e_ < cnt; e_ += blockDim.x)                                         \
         for (int c_ = 0, i_ = (int)(e_ % L.nn[0]), j_ = (int)((e_ / L.nn[0]) % L.nn[1]),                  \
@@ -129,14 +151,20 @@ __global__ void __launch_bounds__(BOT_THREADS) k_bottom(LevelDesc L, BCTable bc,
     const long long n3 = 3 * L.S, cnt = L.count();
     double *r = work, *rh = work + n3, *p = work + 2 * n3, *v = work + 3 * n3, *s = work + 4 * n3,
            *t = work + 5 * n3, *sol = work + 6 * n3, *b = work + 7 * n3;
-
-    // r = (b - A*0)/D, sol = 0
-    double lm = 0;
     FOR_NODES(q)
     {
         b[q] = (double)res[q];
         sol[q] = 0.0;
-        r[q] = b[q] / diag[q];
+    }
+    __syncthreads();
+    const bool sing = L.singular();
+    double mb[3] = {0, 0, 0};
+    if (sing) cta_mean3(L, b, red, mb);
+    // r = P(b - A*0)/D, P the zero-mean projection on a singular level (identity otherwise)
+    double lm = 0;
+    FOR_NODES(q)
+    {
+        r[q] = (b[q] - mb[c_]) / diag[q];
         rh[q] = r[q];
         const double a = fabs(r[q]);
         lm = (a > lm || a != a) ? a : lm;
@@ -160,10 +188,12 @@ __global__ void __launch_bounds__(BOT_THREADS) k_bottom(LevelDesc L, BCTable bc,
             __syncthreads();
             cta_apply<SYM>(L, bc, g, uniform, ddw, p, v);
             __syncthreads();
+            double mv[3] = {0, 0, 0};
+            if (sing) cta_mean3(L, v, red, mv);
             acc = 0;
             FOR_NODES(q)
             {
-                v[q] /= diag[q];
+                v[q] = (v[q] - mv[c_]) / diag[q];
                 acc += rh[q] * v[q];
             }
             const double rhTv = blk_sum(acc, red);
@@ -181,10 +211,12 @@ __global__ void __launch_bounds__(BOT_THREADS) k_bottom(LevelDesc L, BCTable bc,
             if (rnorm < eps_rel * rnorm0 || rnorm < eps_abs) break;
             cta_apply<SYM>(L, bc, g, uniform, ddw, s, t);
             __syncthreads();
+            double mt[3] = {0, 0, 0};
+            if (sing) cta_mean3(L, t, red, mt);
             double tt = 0, ts = 0;
             FOR_NODES(q)
             {
-                t[q] /= diag[q];
+                t[q] = (t[q] - mt[c_]) / diag[q];
                 tt += t[q] * t[q];
                 ts += t[q] * s[q];
             }

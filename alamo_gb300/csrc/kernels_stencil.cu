@@ -335,6 +335,170 @@ __global__ void __launch_bounds__(MT_X* MT_Y) k_stencil_march(LevelDesc L, Geo<T
 }
 
 // ---------------------------------------------------------------------------
+// cp.async-pipelined marching kernel (FP32 cycles on the finest levels)
+//
+// Same tile and per-node arithmetic as k_stencil_march, but the planes are
+// copied global -> shared with 16-byte cp.async (L1 bypassed) two planes ahead
+// of the compute: u in a ring of 4 planes, moduli in a ring of 3, so the loads
+// of plane k+3 overlap the arithmetic of plane k.  Every halo row is 36
+// elements wide and starts at i = 32t, 16-byte aligned (the level's row pitch
+// leaves room for it).  Own-column values at k-1 (moduli) are kept in
+// registers.
+// ---------------------------------------------------------------------------
+constexpr int PT_Z = 32;            // k-chunk of one CTA
+constexpr int PW = 36;              // halo row width loaded (9 x 16 bytes)
+constexpr int PU = 4, PC = 3;       // ring depths (u, moduli)
+
+template <typename T, int SYM> struct PipeSmem {
+    static constexpr int NC = NCoef<SYM>::value;
+    T u[PU][3][MH_Y][PW];
+    T c[PC][NC][MH_Y][PW];
+};
+
+template <typename T, int SYM> struct PipeAcc {
+    const PipeSmem<T, SYM>* s;
+    int tx, ty;            // halo-tile position of the node (1-based)
+    int um, u0, up;        // u ring slots of planes k-1, k, k+1
+    int c0, cp;            // moduli ring slots of planes k, k+1
+    T cm[NCoef<SYM>::value];
+    __device__ __forceinline__ T u(int p, int di, int dj, int dk) const
+    {
+        const int r = dk < 0 ? um : (dk > 0 ? up : u0);
+        return s->u[r][p][ty + dj][tx + di];
+    }
+    __device__ __forceinline__ T C(int m, int di, int dj, int dk) const
+    {
+        if (dk < 0) return cm[m];
+        if (dk > 0) return s->c[cp][m][ty][tx];
+        return s->c[c0][m][ty + dj][tx + di];
+    }
+};
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem)
+{
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    unsigned long long ga;
+    asm volatile("cvta.to.global.u64 %0, %1;" : "=l"(ga) : "l"(gmem));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(ga) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// Queue the copy of plane kk of `ncomp` planes of src into dst[ncomp][MH_Y][PW].
+template <typename T>
+__device__ __forceinline__ void issue_plane(T* dst, const T* __restrict__ src, int ncomp, const LevelDesc& L, int i0,
+                                            int j0, int kk, int tid)
+{
+    constexpr int VEC = 16 / sizeof(T);        // elements per 16-byte chunk
+    constexpr int QPR = PW / VEC;              // chunks per halo row
+    const int per_comp = MH_Y * QPR;
+    const long long plane = (long long)L.P * L.nn[1] * kk;
+    for (int e = tid; e < ncomp * per_comp; e += MT_X * MT_Y) {
+        const int c = e / per_comp, rem = e - c * per_comp;
+        const int row = rem / QPR, q = rem - row * QPR;
+        const int gj = j0 - 1 + row;
+        if (gj > L.n[1]) continue;   // rows past the hi boundary are never read
+        const T* g = src + c * L.S + plane + (long long)L.P * gj + (i0 - 1) + q * VEC;
+        cp_async16(dst + ((c * MH_Y + row) * PW + q * VEC), g);
+    }
+}
+
+template <typename T, int SYM, int MODE>
+__global__ void __launch_bounds__(MT_X* MT_Y) k_stencil_pipe(LevelDesc L, Geo<T> g, int uniform,
+                                                                const T* __restrict__ ddw, const T* __restrict__ x,
+                                                                const T* __restrict__ b, const T* __restrict__ dinv,
+                                                                T* __restrict__ out, T omega, void* norm_slot)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    PipeSmem<T, SYM>& s = *reinterpret_cast<PipeSmem<T, SYM>*>(smem_raw);
+    constexpr int NC = NCoef<SYM>::value;
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + MT_X * ty;
+    const int i0 = 1 + blockIdx.x * MT_X, j0 = 1 + blockIdx.y * MT_Y;
+    const int k0 = 1 + blockIdx.z * PT_Z;
+    const int k1 = min(k0 + PT_Z, L.n[2]);   // exclusive
+    const int i = i0 + tx, j = j0 + ty;
+    const bool mine = (i < L.n[0]) && (j < L.n[1]);
+    const long long S = L.S;
+
+    PipeAcc<T, SYM> acc;
+    acc.s = &s;
+    acc.tx = tx + 1;
+    acc.ty = ty + 1;
+    {
+        const long long p = L.idx(min(i, L.n[0]), min(j, L.n[1]), k0 - 1);
+#pragma unroll
+        for (int m = 0; m < NC; m++) acc.cm[m] = __ldg(ddw + m * S + p);
+    }
+    // prologue: planes k0-1, k0, k0+1 of u and k0, k0+1 of the moduli, then k0+2
+    issue_plane<T>(&s.u[0][0][0][0], x, 3, L, i0, j0, k0 - 1, tid);
+    issue_plane<T>(&s.u[1][0][0][0], x, 3, L, i0, j0, k0, tid);
+    issue_plane<T>(&s.u[2][0][0][0], x, 3, L, i0, j0, k0 + 1, tid);
+    issue_plane<T>(&s.c[0][0][0][0], ddw, NC, L, i0, j0, k0, tid);
+    issue_plane<T>(&s.c[1][0][0][0], ddw, NC, L, i0, j0, k0 + 1, tid);
+    cp_async_commit();
+    if (k0 + 2 <= k1) {
+        issue_plane<T>(&s.u[3][0][0][0], x, 3, L, i0, j0, k0 + 2, tid);
+        issue_plane<T>(&s.c[2][0][0][0], ddw, NC, L, i0, j0, k0 + 2, tid);
+    }
+    cp_async_commit();
+
+    T nrm = 0;
+    for (int k = k0; k < k1; k++) {
+        const int it = k - k0;
+        long long q = 0;
+        T bq[3] = {0, 0, 0}, dq[3] = {0, 0, 0};
+        if (mine) {
+            q = L.idx(i, j, k);
+            if (MODE != MODE_APPLY)
+#pragma unroll
+                for (int c = 0; c < 3; c++) bq[c] = __ldg(b + c * S + q);
+            if (MODE == MODE_JACOBI)
+#pragma unroll
+                for (int c = 0; c < 3; c++) dq[c] = __ldg(dinv + c * S + q);
+        }
+        cp_async_wait1();
+        __syncthreads();
+        acc.um = it % PU;
+        acc.u0 = (it + 1) % PU;
+        acc.up = (it + 2) % PU;
+        acc.c0 = it % PC;
+        acc.cp = (it + 1) % PC;
+        if (mine) {
+            T f[3];
+            interior_row<T, SYM>(acc, g, uniform != 0, f);
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                const long long o = c * S + q;
+                if (MODE == MODE_APPLY) {
+                    out[o] = f[c];
+                } else if (MODE == MODE_RESID) {
+                    const T r = bq[c] - f[c];
+                    out[o] = r;
+                    const T a = fabs(r);
+                    nrm = (a > nrm || a != a) ? a : nrm;
+                } else {
+                    const T xc = s.u[acc.u0][c][ty + 1][tx + 1];
+                    out[o] = xc + omega * ((bq[c] - f[c]) * dq[c]);
+                }
+            }
+        }
+#pragma unroll
+        for (int m = 0; m < NC; m++) acc.cm[m] = s.c[acc.c0][m][ty + 1][tx + 1];
+        __syncthreads();
+        // refill the slots of u(k-1) and C(k) with plane k+3
+        const int kk = k + 3;
+        if (kk <= k1) {
+            issue_plane<T>(&s.u[it % PU][0][0][0], x, 3, L, i0, j0, kk, tid);
+            issue_plane<T>(&s.c[it % PC][0][0][0], ddw, NC, L, i0, j0, kk, tid);
+        }
+        cp_async_commit();
+    }
+    cp_async_wait0();
+    if (MODE == MODE_RESID && norm_slot) block_max_to_slot<T>(nrm, norm_slot);
+}
+
+// ---------------------------------------------------------------------------
 // diagonal
 // ---------------------------------------------------------------------------
 template <typename T, int SYM>
@@ -375,6 +539,16 @@ int march_min_cells()
     return v;
 }
 
+// FP32 interiors use the cp.async-pipelined kernel unless AGB_PIPE=0.
+bool use_pipe_kernel()
+{
+    static bool v = [] {
+        const char* s = getenv("AGB_PIPE");
+        return !(s && s[0] == '0');
+    }();
+    return v;
+}
+
 template <typename T, int SYM, int MODE>
 static void stencil_dispatch(cudaStream_t st, const LevelDesc& L, const BCTable& bc, bool uniform, const T* ddw,
                              const T* x, const T* b, const T* diag, T* out, T omega, void* norm_slot)
@@ -386,11 +560,19 @@ static void stencil_dispatch(cudaStream_t st, const LevelDesc& L, const BCTable&
                      L.n[1] >= 16 && L.n[2] >= 16;
     if (big) {
         // interior by the marching kernel, boundary shell by the per-node kernel
-        const size_t smem = sizeof(MarchSmem<T, SYM>);
         dim3 blk(MT_X, MT_Y, 1);
-        dim3 grd((L.n[0] - 1 + MT_X - 1) / MT_X, (L.n[1] - 1 + MT_Y - 1) / MT_Y, (L.n[2] - 1 + MT_Z - 1) / MT_Z);
-        k_stencil_march<T, SYM, MODE><<<grd, blk, smem, st>>>(L, g, uniform ? 1 : 0, ddw, x, b, diag, out, omega,
-                                                                norm_slot); count_launch();
+        if (sizeof(T) == 4 && use_pipe_kernel()) {
+            const size_t smem = sizeof(PipeSmem<T, SYM>);
+            dim3 grd((L.n[0] - 1 + MT_X - 1) / MT_X, (L.n[1] - 1 + MT_Y - 1) / MT_Y, (L.n[2] - 1 + PT_Z - 1) / PT_Z);
+            k_stencil_pipe<T, SYM, MODE><<<grd, blk, smem, st>>>(L, g, uniform ? 1 : 0, ddw, x, b, diag, out, omega,
+                                                                   norm_slot);
+        } else {
+            const size_t smem = sizeof(MarchSmem<T, SYM>);
+            dim3 grd((L.n[0] - 1 + MT_X - 1) / MT_X, (L.n[1] - 1 + MT_Y - 1) / MT_Y, (L.n[2] - 1 + MT_Z - 1) / MT_Z);
+            k_stencil_march<T, SYM, MODE><<<grd, blk, smem, st>>>(L, g, uniform ? 1 : 0, ddw, x, b, diag, out, omega,
+                                                                    norm_slot);
+        }
+        count_launch();
         const long long ns = shell_count(L);
         k_stencil_shell<T, SYM, MODE><<<(unsigned)((ns + 255) / 256), 256, 0, st>>>(L, bc, g, ddw, x, b, diag, out,
                                                                                     omega, norm_slot);
@@ -427,6 +609,12 @@ static void set_attr()
     cudaFuncSetAttribute(k_stencil_march<T, SYM, MODE_APPLY>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     cudaFuncSetAttribute(k_stencil_march<T, SYM, MODE_RESID>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     cudaFuncSetAttribute(k_stencil_march<T, SYM, MODE_JACOBI>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (sizeof(T) == 4) {
+        const int ps = (int)sizeof(PipeSmem<T, SYM>);
+        cudaFuncSetAttribute(k_stencil_pipe<T, SYM, MODE_APPLY>, cudaFuncAttributeMaxDynamicSharedMemorySize, ps);
+        cudaFuncSetAttribute(k_stencil_pipe<T, SYM, MODE_RESID>, cudaFuncAttributeMaxDynamicSharedMemorySize, ps);
+        cudaFuncSetAttribute(k_stencil_pipe<T, SYM, MODE_JACOBI>, cudaFuncAttributeMaxDynamicSharedMemorySize, ps);
+    }
 }
 
 // Opt the marching kernels into their shared-memory size; called once per

@@ -218,6 +218,44 @@ __global__ void k_recip(long long n, const double* __restrict__ d, TD* __restric
         r[e] = d[e] != 0.0 ? (TD)(1.0 / d[e]) : (TD)0;
 }
 
+// per-component sums over the stored nodes (sums[0..2], accumulated) or, with
+// `subtract`, x -= sums / count: the zero-mean normalization of a fully
+// periodic box's displacement
+template <typename T>
+__global__ void k_mean3(LevelDesc L, T* __restrict__ x, double* __restrict__ sums, int subtract, void* norm_slot)
+{
+    const long long cnt = L.count();
+    double s[3] = {0, 0, 0};
+    T m = 0;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < cnt; e += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(e % L.nn[0]), j = (int)((e / L.nn[0]) % L.nn[1]),
+                  k = (int)(e / ((long long)L.nn[0] * L.nn[1]));
+        const long long q = L.idx(i, j, k);
+        for (int c = 0; c < 3; c++) {
+            if (subtract) {
+                const T v = (T)((double)x[c * L.S + q] - sums[c] / (double)cnt);
+                x[c * L.S + q] = v;
+                const T a = fabs(v);
+                m = (a > m || a != a) ? a : m;
+            } else s[c] += (double)x[c * L.S + q];
+        }
+    }
+    if (subtract) {
+        if (!norm_slot) return;
+        for (int o = 16; o > 0; o >>= 1) {
+            const T w = __shfl_xor_sync(0xffffffffu, m, o);
+            m = (w > m || w != w) ? w : m;
+        }
+        if ((threadIdx.x & 31) == 0) MaxSlot<T>::put(norm_slot, m);
+        return;
+    }
+    for (int c = 0; c < 3; c++) {
+        double v = s[c];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0) atomicAdd(&sums[c], v);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
@@ -294,6 +332,17 @@ void launch_export(cudaStream_t st, const LevelDesc& L, int ncomp, const TS* src
     k_export<TD, TS><<<grd, blk, 0, st>>>(L, ncomp, src, dst, aos ? 1 : 0, k0, kc, chunk ? 1 : 0); count_launch();
 }
 
+template <typename T>
+void launch_remove_mean(cudaStream_t st, const LevelDesc& L, T* x, double* sums3, void* norm_slot)
+{
+    cudaMemsetAsync(sums3, 0, 3 * sizeof(double), st);
+    const int g = blocks_1d(L.count());
+    k_mean3<T><<<g, 256, 0, st>>>(L, x, sums3, 0, nullptr);
+    count_launch();
+    k_mean3<T><<<g, 256, 0, st>>>(L, x, sums3, 1, norm_slot);
+    count_launch();
+}
+
 void launch_axpy_mixed(cudaStream_t st, const LevelDesc& L, int ncomp, double* y, const float* x, double a)
 {
     const long long n = (long long)ncomp * L.S;
@@ -315,6 +364,7 @@ void launch_recip(cudaStream_t st, const LevelDesc& L, int ncomp, const double* 
     template void launch_zero<T>(cudaStream_t, const LevelDesc&, int, T*);                                   \
     template void launch_norm_inf<T>(cudaStream_t, const LevelDesc&, int, const T*, void*);                  \
     template void launch_recip<T>(cudaStream_t, const LevelDesc&, int, const double*, T*);                   \
+    template void launch_remove_mean<T>(cudaStream_t, const LevelDesc&, T*, double*, void*);                 \
     template void launch_import<T, double>(cudaStream_t, const LevelDesc&, int, const double*, T*, bool, int, int, bool); \
     template void launch_import<T, float>(cudaStream_t, const LevelDesc&, int, const float*, T*, bool, int, int, bool);   \
     template void launch_export<T, double>(cudaStream_t, const LevelDesc&, int, const double*, T*, bool, int, int, bool); \

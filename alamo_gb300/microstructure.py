@@ -124,6 +124,53 @@ def voronoi_grain_ids(n, pts):
     return ids.reshape(-1)
 
 
+RVE_EDGES = (32, 48, 64, 80, 96)
+
+
+def rve_problem(q, seed=4242, edges=RVE_EDGES, contrast_max=10.0, width=1.5):
+    """Periodic RVE number q of a batch: edge uniform in `edges` cells, 1-8
+    ellipsoidal isotropic inclusions (semi-axes 0.05-0.2 of the edge, random
+    orientation, periodic images) with stiffness contrast log-uniform in
+    [1, contrast_max], matrix lambda = mu = 1, and a macroscopic strain with
+    symmetric entries U(+-1e-3) applied as the uniform eigenstrain F0 = -strain.
+
+    The inclusion boundary is diffuse: log(contrast) follows a tanh profile of
+    `width` cells across the approximate distance to the ellipsoid surface, as
+    a phase-field microstructure would give.  The operator's grad(C) term is a
+    central difference, and a stiffness jump of tens across one cell makes it
+    lose diagonal dominance: the damped-Jacobi multigrid then diverges on the
+    same material with any boundary condition, so sharp inclusions are not a
+    usable workload for this solver.
+    Returns (n, ddw AoS (lambda, mu) on the (n+1)^3 nodal box, F0 (3x3))."""
+    rng = SplitMix64(seed * 1000003 + q)
+    n = int(edges[min(int(rng.uniform() * len(edges)), len(edges) - 1)])
+    x = np.arange(n + 1) / n
+    Z, Y, X = np.meshgrid(x, x, x, indexing="ij")
+    P = np.stack([X, Y, Z], axis=-1).reshape(-1, 3)
+    logc = np.zeros(P.shape[0])
+    ninc = 1 + min(int(rng.uniform() * 8), 7)
+    for _ in range(ninc):
+        c = np.array([rng.uniform() for _ in range(3)])
+        axes = np.array([0.05 + 0.15 * rng.uniform() for _ in range(3)])
+        R = quat_to_rot([rng.normal() for _ in range(4)])
+        lk = np.log(contrast_max) * rng.uniform()
+        d = P - c
+        d -= np.round(d)              # nearest periodic image
+        y = d @ R                     # components in the inclusion frame
+        r = np.sqrt(np.sum((y / axes) ** 2, axis=1))
+        s = (r - 1.0) * axes.mean()   # approximate distance to the surface
+        phi = 0.5 * (1.0 - np.tanh(s * n / width))
+        logc = np.maximum(logc, phi * lk)
+    contrast = np.exp(logc)
+    ddw = np.empty((P.shape[0], 2))
+    ddw[:, 0] = contrast
+    ddw[:, 1] = contrast
+    e = np.zeros((3, 3))
+    for a, b in ((0, 0), (1, 1), (2, 2), (0, 1), (0, 2), (1, 2)):
+        e[a, b] = e[b, a] = (2.0 * rng.uniform() - 1.0) * 1e-3
+    return n, ddw.reshape(-1), -e
+
+
 def voronoi_cubic(n=256, ngrains=64, seed=20260, C11=1.68, C12=1.21, C44=0.75):
     """Returns (ddw AoS 21 per node, grain ids, table)."""
     pts, table = voronoi_seeds(ngrains, seed, C11, C12, C44)

@@ -174,6 +174,34 @@ agb_status agb_newton_solve(agb_solver s, const double* F0, double* u, const dou
 agb_status agb_stress(agb_op op, const double* F0, const double* u, double* sigma9, int mem);
 agb_status agb_traction_xhi(agb_op op, const double* F0, const double* u, double trac[3], int mem);
 
+/* Batched RVE homogenization: `nprob` independent boxes (sizes n_cells[3*q..],
+ * cell sizes dx[3*q..]; periodic in the directions of `periodic`, NULL = all)
+ * solved together -- one persistent launch per multigrid step for the whole
+ * batch, each V-cycle replayed from a captured CUDA graph, tile shapes picked
+ * by timing on the batch at the first solve.  Each problem's right-hand side is
+ * the Newton step at u = 0 of an affine model with a uniform eigenstrain F0
+ * (9 doubles per problem; F0 = -macroscopic strain), the setting of
+ * Model/Solid/Affine with Newton.H:199-231.  Per problem the algorithm is the
+ * single-box solver's, V-cycles; params.precision selects plain FP64 or FP32
+ * cycles in FP64 refinement.  For fully periodic boxes the solution is returned
+ * modulo rigid translation (zero mean). */
+typedef struct agb_batch_s* agb_batch;
+agb_status agb_batch_create(int nprob, const int* n_cells, const double* dx, const int periodic[3], int sym,
+                            const agb_solver_params* params, agb_batch* out);
+agb_status agb_batch_destroy(agb_batch b);
+agb_status agb_batch_set_bc(agb_batch b, const agb_bc* bc);
+agb_status agb_batch_set_model(agb_batch b, int prob, const double* ddw, int layout, int mem);
+agb_status agb_batch_set_eigenstrain(agb_batch b, const double* F0);
+/* reports: one per problem (may be NULL); total: iterations = max over problems,
+ * res_final = max relative residual, solve_ms, kernels. */
+agb_status agb_batch_solve(agb_batch b, double tol_rel, double tol_abs, agb_solve_report* reports,
+                           agb_solve_report* total);
+agb_status agb_batch_get_solution(agb_batch b, int prob, double* u, int mem);
+/* volume-averaged stress C : (grad u - F0) per problem (9 doubles, host) */
+agb_status agb_batch_mean_stress(agb_batch b, double* sigma);
+/* the stencil tile shape the autotuner chose for a level */
+agb_status agb_batch_tuning(agb_batch b, int level, int dims[3]);
+
 /* Timing hook used by the benchmark: runs `reps` launches of one internal
  * stencil sweep (mode 0 apply, 1 residual, 2 Jacobi) at `level` in FP64
  * (precision AGB_PREC_F64) or FP32 (AGB_PREC_MIXED) on the operator's resident

@@ -855,14 +855,46 @@ static double dotxy(const orc_grid* g, const double* x, const double* y)
     return s;
 }
 
+static int fully_periodic(const orc_grid* g) { return g->periodic[0] && g->periodic[1] && g->periodic[2]; }
+
+/* Subtract the per-component mean over the unique nodes (periodic images
+ * counted once).
+ *
+ * A fully periodic box has the rigid translations as null space.  The
+ * reference has no fully periodic elastic solve (its operator is never
+ * singular, Operator.H:96-97); this project's periodic RVE solves follow the
+ * idea of MLMG's makeSolvable instead: the right-hand side and every
+ * fine-level residual are projected to zero mean, and so are the residual and
+ * every operator application of the bottom Krylov solve.  Because the
+ * operator is not conservative its left null vectors are constants only up to
+ * discretisation error, so the solve finds u with  A u = b - c  for a uniform
+ * body force c (per component) of the size of that error, rather than
+ * A u = b.  The returned displacement has zero mean. */
+static void remove_mean(const orc_grid* g, double* v)
+{
+    const long N = orc_nnodes(g);
+    const long cnt = (long)g->n[0] * g->n[1] * g->n[2];
+    for (int c = 0; c < 3; c++) {
+        double s = 0.0;
+        for (int k = 0; k < g->n[2]; k++)
+            for (int j = 0; j < g->n[1]; j++)
+                for (int i = 0; i < g->n[0]; i++) s += v[c * N + IDX(g, i, j, k)];
+        const double mean = s / (double)cnt;
+        for (long q = 0; q < N; q++) v[c * N + q] -= mean;
+    }
+}
+
 /*
  * BiCGStab on the diagonally scaled system (MLCGSolver::solve_bicgstab with
  * Operator<Node>::normalize = divide by the diagonal, Operator.cpp:156-165).
- * Returns 0 converged, 1..4 breakdown, 8 not converged.
+ * Returns 0 converged, 1..4 breakdown, 8 not converged.  On a fully periodic
+ * box the residual and each operator application are projected to zero mean
+ * before the scaling (see remove_mean).
  */
 static int bottom_bicgstab(mg_t* m, int l, double* sol, const double* rhs)
 {
     const orc_grid* g = &m->g[l];
+    const int sing = fully_periodic(g);
     const long n3 = 3 * m->N[l];
     const double* D = m->diag[l];
     const double eps_rel = m->p->bottom_tol_rel, eps_abs = m->p->bottom_tol_abs;
@@ -870,6 +902,7 @@ static int bottom_bicgstab(mg_t* m, int l, double* sol, const double* rhs)
     double *r = buf, *rh = buf + n3, *p = buf + 2 * n3, *v = buf + 3 * n3, *s = buf + 4 * n3,
            *t = buf + 5 * n3, *sorig = buf + 6 * n3;
     orc_residual(g, m->ddw[l], sol, rhs, r);
+    if (sing) remove_mean(g, r);
     for (long q = 0; q < n3; q++) r[q] /= D[q];
     for (long q = 0; q < n3; q++) { sorig[q] = sol[q]; sol[q] = 0.0; rh[q] = r[q]; }
     double rnorm = orc_norm_inf(g, r);
@@ -891,6 +924,7 @@ static int bottom_bicgstab(mg_t* m, int l, double* sol, const double* rhs)
             for (long q = 0; q < n3; q++) p[q] = r[q] + beta * (p[q] - omega * v[q]);
         }
         orc_fapply(g, m->ddw[l], p, v);
+        if (sing) remove_mean(g, v);
         for (long q = 0; q < n3; q++) v[q] /= D[q];
         double rhTv = dotxy(g, rh, v);
         if (rhTv != 0) alpha = rho / rhTv;
@@ -899,6 +933,7 @@ static int bottom_bicgstab(mg_t* m, int l, double* sol, const double* rhs)
         rnorm = orc_norm_inf(g, s);
         if (rnorm < eps_rel * rnorm0 || rnorm < eps_abs) break;
         orc_fapply(g, m->ddw[l], s, t);
+        if (sing) remove_mean(g, t);
         for (long q = 0; q < n3; q++) t[q] /= D[q];
         double tt = dotxy(g, t, t), ts = dotxy(g, t, s);
         if (tt != 0) omega = ts / tt;
@@ -992,7 +1027,17 @@ int orc_solve(const orc_grid* g, const double* ddw, const orc_solver_params* p,
     for (int l = 1; l < m.L; l++) orc_average_ddw(&m.g[l - 1], m.ddw[l - 1], m.ddw[l]);
     for (int l = 0; l < m.L; l++) orc_diagonal(&m.g[l], m.ddw[l], m.diag[l]);
 
+    /* fully periodic box: solve with the zero-mean part of b (see remove_mean) */
+    const int sing = fully_periodic(g);
+    double* bproj = NULL;
+    if (sing) {
+        bproj = (double*)malloc(sizeof(double) * 3 * m.N[0]);
+        memcpy(bproj, b, sizeof(double) * 3 * m.N[0]);
+        remove_mean(g, bproj);
+        b = bproj;
+    }
     orc_residual(&m.g[0], m.ddw[0], x, b, m.res[0]);
+    if (sing) remove_mean(g, m.res[0]);
     const double resnorm0 = orc_norm_inf(g, m.res[0]);
     const double rhsnorm0 = orc_norm_inf(g, b);
     const double max_norm = (rhsnorm0 >= resnorm0) ? rhsnorm0 : resnorm0;
@@ -1013,6 +1058,7 @@ int orc_solve(const orc_grid* g, const double* ddw, const orc_solver_params* p,
             else mg_vcycle(&m, 0);
             for (long q = 0; q < n3; q++) x[q] += m.cor[0][q];
             orc_residual(&m.g[0], m.ddw[0], x, b, m.res[0]);
+            if (sing) remove_mean(g, m.res[0]);
             norm = orc_norm_inf(g, m.res[0]);
             rep->iterations = iter + 1;
             if (p->verbose) fprintf(stderr, "oracle MLMG iter %d resid %.6e rel %.6e\n", iter + 1, norm, norm / max_norm);
@@ -1022,11 +1068,13 @@ int orc_solve(const orc_grid* g, const double* ddw, const orc_solver_params* p,
         }
     }
     rep->res_final = norm;
+    if (sing) remove_mean(g, x);   /* solution modulo rigid translation */
     rep->t_iter = omp_get_wtime() - t1;
     for (int l = 0; l < m.L; l++) {
         if (l > 0) free(m.ddw[l]);
         free(m.diag[l]); free(m.cor[l]); free(m.res[l]); free(m.rescor[l]); free(m.hold[l]);
     }
+    free(bproj);
     return rep->status;
 }
 
