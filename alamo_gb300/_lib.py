@@ -127,6 +127,9 @@ def lib():
         "agb_batch_get_solution": (st, [vp, ctypes.c_int, vp, ctypes.c_int]),
         "agb_batch_mean_stress": (st, [vp, dp]),
         "agb_batch_tuning": (st, [vp, ctypes.c_int, ip]),
+        "agb_bottom_solve_noalloc": (st, [ip, dp, ctypes.c_int, ctypes.c_int, ctypes.POINTER(AgbBC), vp, vp, vp, vp,
+                                          vp, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                          ctypes.c_int, ctypes.c_double, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

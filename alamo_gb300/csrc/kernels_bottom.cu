@@ -288,3 +288,126 @@ template void launch_bottom<float>(cudaStream_t, int, const LevelDesc&, const BC
                                    double);
 
 }  // namespace agb
+
+// ---------------------------------------------------------------------------
+// Allocation-free coarsest-level solve (agb_bottom_solve_noalloc in agb.h)
+//
+// Some callers may not allocate device memory at the moment they need a
+// bottom solve: a host framework that owns every device byte through its own
+// arena and forbids cudaMalloc inside its solver hooks, or code that runs
+// while a stream is being captured into a CUDA graph.  For them the BiCGStab
+// work vectors live in a file-scope device array instead of a buffer of an
+// operator handle.  The array is sized for boxes of at most
+// AGB_NOALLOC_MAX_NODES nodes (a 16^3-cell box); every GPU that loads this
+// library holds it (943 KB) until the process exits.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+#include "agb.h"
+
+namespace {
+
+constexpr long long kScratchDoubles = 8LL * 3LL * AGB_NOALLOC_MAX_NODES;
+static __device__ __align__(256) double g_bottom_scratch[kScratchDoubles];
+
+constexpr int kMaxDevices = 256;
+std::mutex g_scratch_mutex;
+double* g_scratch_addr[kMaxDevices] = {nullptr};
+
+// Device address of g_bottom_scratch on the current device.  The name
+// g_bottom_scratch is only a host-side stand-in: a kernel must be given the
+// address that cudaGetSymbolAddress returns for the device it runs on.
+agb_status scratch_for_current_device(double** out)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) {
+        agb::set_error("no usable CUDA device for the allocation-free bottom solve");
+        return AGB_CUDA;
+    }
+    if (dev < 0 || dev >= kMaxDevices) {
+        agb::set_error("device index out of range");
+        return AGB_CUDA;
+    }
+    std::lock_guard<std::mutex> lock(g_scratch_mutex);
+    if (!g_scratch_addr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_bottom_scratch);
+        if (e != cudaSuccess || !p) {
+            agb::set_error("cudaGetSymbolAddress of the bottom-solve scratch failed");
+            return AGB_CUDA;
+        }
+        g_scratch_addr[dev] = (double*)p;
+    }
+    *out = g_scratch_addr[dev];
+    return AGB_OK;
+}
+
+}  // namespace
+
+extern "C" agb_status agb_bottom_solve_noalloc(const int n_cells[3], const double dx[3], int sym, int uniform,
+                                               const agb_bc* bc, const double* ddw, const double* diag,
+                                               const double* res, double* cor, int* ret, int max_iter,
+                                               double tol_rel, double tol_abs, int bottom_smooth, int final_smooth,
+                                               double omega, void* stream)
+{
+    using namespace agb;
+    if (!n_cells || !dx || !bc || !ddw || !diag || !res || !cor || !ret) {
+        set_error("null argument");
+        return AGB_BADARG;
+    }
+    if (sym != AGB_ISO && sym != AGB_MAJORMINOR) {
+        set_error("sym must be AGB_ISO or AGB_MAJORMINOR");
+        return AGB_BADARG;
+    }
+    long long nodes = 1;
+    for (int d = 0; d < 3; d++) {
+        if (n_cells[d] < 1 || !(dx[d] > 0)) {
+            set_error("n_cells must be >= 1 and dx > 0");
+            return AGB_BADARG;
+        }
+        nodes *= (long long)(n_cells[d] + 1);
+    }
+    if (nodes > AGB_NOALLOC_MAX_NODES) {
+        set_error("box too large for the allocation-free bottom solve: more than AGB_NOALLOC_MAX_NODES nodes");
+        return AGB_BADARG;
+    }
+    if (max_iter < 0 || bottom_smooth < 0 || final_smooth < 0 || !(omega > 0 && omega < 2)) {
+        set_error("bad iteration count, smoothing count or omega");
+        return AGB_BADARG;
+    }
+    BCTable t;
+    for (int f = 0; f < F_NFACES; f++)
+        for (int c = 0; c < 3; c++) {
+            if (bc->type[f][c] < AGB_BC_DISP || bc->type[f][c] > AGB_BC_NONE) {
+                set_error("bad BC type");
+                return AGB_BADARG;
+            }
+            t.type[f][c] = (int8_t)bc->type[f][c];
+            t.val[f][c] = bc->val[f][c];
+        }
+    // The caller's arrays are the unpadded reference layout: row pitch n0+1,
+    // component stride = node count.
+    LevelDesc L;
+    for (int d = 0; d < 3; d++) {
+        L.n[d] = n_cells[d];
+        L.nn[d] = n_cells[d] + 1;
+        L.per[d] = 0;
+        L.dx[d] = dx[d];
+    }
+    L.P = L.nn[0];
+    L.S = nodes;
+    double* work = nullptr;
+    const agb_status s = scratch_for_current_device(&work);
+    if (s != AGB_OK) return s;
+    // Every scratch element the kernel reads is written earlier in the same
+    // launch, so the contents left by a previous call need no clearing.
+    launch_bottom<double>((cudaStream_t)stream, sym, L, t, uniform != 0, ddw, diag, cor, res, work, max_iter, tol_rel,
+                          tol_abs, ret, bottom_smooth, final_smooth, omega);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_error(cudaGetErrorString(e));
+        return AGB_CUDA;
+    }
+    return AGB_OK;
+}

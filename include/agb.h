@@ -213,6 +213,37 @@ agb_status agb_op_time_sweep(agb_op op, int level, int precision, int mode, int 
 agb_status agb_host_alloc(size_t bytes, void** p);
 agb_status agb_host_free(void* p);
 
+/* Allocation-free coarsest-level solve.  No counterpart in the reference: it
+ * exists for callers that may not allocate device memory when they need a
+ * bottom solve -- a host framework that owns all device memory through its
+ * own arena and forbids cudaMalloc inside solver hooks, or code running while
+ * a stream is captured.  It computes what the solve's bottom step computes
+ * (BiCGStab on the diagonally scaled system, then smoothing) for one box with
+ * no periodic direction, without calling cudaMalloc, cudaFree or any
+ * allocating routine: its work vectors live in a device array of the library
+ * sized for AGB_NOALLOC_MAX_NODES nodes (a 16^3-cell box), which every GPU that
+ * loads the library keeps (943 KB) until the process exits.
+ *   - All array arguments are DEVICE pointers in the unpadded reference
+ *     layout: ddw coefficient-major (AGB_LAYOUT_SOA), diag / res / cor with the
+ *     three components one after the other; *ret receives the BiCGStab code
+ *     (0 converged, 1-4 breakdown, 8 not converged).
+ *   - Larger boxes are rejected with AGB_BADARG.
+ *   - The work is queued on `stream` (a cudaStream_t; NULL = default stream)
+ *     and the call returns without waiting: results are valid once that
+ *     stream has been synchronized.
+ *   - The first call on a device looks up the array's device address (once
+ *     per device, with that device current); make that first call before any
+ *     stream capture.
+ *   - Every call shares the one array: calls whose work overlaps on the GPU
+ *     (several streams, several host threads) race and corrupt each other.
+ *     Each call writes every scratch element before reading it, so nothing
+ *     left by an earlier call leaks into a result. */
+#define AGB_NOALLOC_MAX_NODES 4913
+agb_status agb_bottom_solve_noalloc(const int n_cells[3], const double dx[3], int sym, int uniform,
+                                    const agb_bc* bc, const double* ddw, const double* diag, const double* res,
+                                    double* cor, int* ret, int max_iter, double tol_rel, double tol_abs,
+                                    int bottom_smooth, int final_smooth, double omega, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,95 @@
+"""GPU: the allocation-free bottom solve (agb_bottom_solve_noalloc).
+
+Callers that may not allocate device memory when they need a coarsest-level
+solve (a framework that owns every device byte through its own arena, or code
+running under stream capture) use this entry point; its work vectors live in
+a fixed device array of the library.  This test calls it through the C ABI
+twice in a row on device buffers and checks each result against the existing
+entry point that performs the same computation: agb_solve on a one-level
+operator with exactly one iteration, whose single cycle is the bottom solve.
+It also checks that a box above the array's size limit is refused.
+
+The file name sorts last so that a run stopping at the first failure has run
+every other test before this one.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12
+
+
+def problem(n):
+    from alamo_gb300 import microstructure as M
+    from alamo_gb300.elastic import TensionTest
+    ddw, F0 = M.sphere_inclusion(n)
+    bc = TensionTest("uniaxial_stress", disp=0.01)
+    g = O.make_grid([n] * 3, sym=O.ISO, bc_type=bc.type, bc_val=bc.val)
+    N = O.nodes(g)
+    b = O.bc_init(g, np.zeros(3 * N))
+    rhs = O.newton_rhs(g, ddw, F0, np.zeros(3 * N), b)
+    return ddw, bc, rhs
+
+
+def call_noalloc(n, ddw_soa, diag, rhs, bc, params, out, ret):
+    from alamo_gb300 import _lib
+    L = _lib.lib()
+    return L.agb_bottom_solve_noalloc(
+        (ctypes.c_int * 3)(n, n, n), (ctypes.c_double * 3)(1.0 / n, 1.0 / n, 1.0 / n), _lib.AGB_ISO, 0,
+        ctypes.byref(bc.to_c()), ctypes.c_void_p(ddw_soa.data_ptr()), ctypes.c_void_p(diag.data_ptr()),
+        ctypes.c_void_p(rhs.data_ptr()), ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(ret.data_ptr()),
+        params.bottom_max_iter, params.bottom_tol_rel, params.bottom_tol_abs, params.bottom_smooth,
+        params.final_smooth, 2.0 / 3.0, None)
+
+
+def test_noalloc_bottom_matches_existing_entry_point(gpu_lib):
+    torch = pytest.importorskip("torch")
+    from alamo_gb300 import Elastic, Linear, default_params
+    from alamo_gb300._lib import AGB_OK, check
+    n = 8
+    ddw, bc, rhs = problem(n)
+    op = Elastic([n] * 3, None, "isotropic", max_coarsening_level=0)
+    assert op.NumLevels() == 1
+    op.SetBC(bc)
+    op.SetModel(ddw)
+    # existing entry point: one MLMG iteration of a one-level hierarchy = one bottom solve
+    ref = np.zeros_like(rhs)
+    s = Linear(op, fixed_iter=1, max_iter=1)
+    s.solve(ref, rhs, 1e-30, 0.0)
+    assert s.report.iterations == 1
+    diag = op.Diagonal(0)
+    N = (n + 1) ** 3
+    ddw_soa = np.ascontiguousarray(op.GetModel(0).reshape(N, 2).T).reshape(-1)
+    d_ddw = torch.from_numpy(ddw_soa).cuda()
+    d_diag = torch.from_numpy(diag).cuda()
+    d_rhs = torch.from_numpy(rhs).cuda()
+    d_ret = torch.full((1,), -1, dtype=torch.int32, device="cuda")
+    p = default_params()
+    for call in range(2):
+        d_out = torch.full((3 * N,), float("nan"), dtype=torch.float64, device="cuda")
+        check(call_noalloc(n, d_ddw, d_diag, d_rhs, bc, p, d_out, d_ret))
+        torch.cuda.synchronize()
+        out = d_out.cpu().numpy()
+        assert int(d_ret.item()) in (0, 8)
+        err = np.abs(out - ref).max() / np.abs(ref).max()
+        assert err < TOL, (call, err)
+    s.Clear()
+    op.close()
+
+
+def test_noalloc_rejects_oversize(gpu_lib):
+    torch = pytest.importorskip("torch")
+    from alamo_gb300 import default_params
+    from alamo_gb300._lib import AGB_BADARG
+    from alamo_gb300.elastic import Constant
+    n = 17  # 18^3 nodes > AGB_NOALLOC_MAX_NODES
+    N = (n + 1) ** 3
+    z = torch.zeros(3 * N, dtype=torch.float64, device="cuda")
+    zc = torch.zeros(2 * N, dtype=torch.float64, device="cuda")
+    r = torch.zeros(1, dtype=torch.int32, device="cuda")
+    assert call_noalloc(n, zc, z, z, Constant(), default_params(), z, r) == AGB_BADARG
