@@ -94,6 +94,7 @@ struct agb_op_s {
     double* d_slots = nullptr;   // 16 x 8 bytes of reduction slots
     double* h_slots = nullptr;   // pinned mirror
     double* bottom_work = nullptr;
+    double* bottom_A = nullptr;   // dense coarsest-level operator (small bottom levels)
     int* d_ret = nullptr;
     char* stage = nullptr;       // bounded staging buffer for pageable host copies
     size_t stage_bytes = 0;
@@ -258,6 +259,9 @@ agb_status prepare(agb_op op)
         launch_diagonal<double>(op->st, op->sym, lv.L, op->bc, lv.ddw64, lv.diag64);
         launch_recip<double>(op->st, lv.L, 3, lv.diag64, lv.dinv64);
     }
+    if (op->bottom_A)
+        launch_bottom_assemble(op->st, op->sym, op->lev.back().L, op->bc, op->uniform, op->lev.back().ddw64,
+                               op->bottom_A);
     CK(cudaGetLastError());
     op->prepared = true;
     op->f32_ready = false;
@@ -329,6 +333,12 @@ template <typename T> struct Engine {
     void bottom()
     {
         Level& v = lv(bot());
+        if (op->bottom_A) {
+            launch_bottom_dense<T>(op->st, v.L, op->bottom_A, v.diag64, A::cor(v), A::res(v), p.bottom_max_iter,
+                                   p.bottom_tol_rel, p.bottom_tol_abs, op->d_ret, p.bottom_smooth, p.final_smooth,
+                                   op->omega);
+            return;
+        }
         launch_bottom<T>(op->st, op->sym, v.L, op->bc, op->uniform, v.ddw64, v.diag64, A::cor(v), A::res(v),
                          op->bottom_work, p.bottom_max_iter, p.bottom_tol_rel, p.bottom_tol_abs, op->d_ret,
                          p.bottom_smooth, p.final_smooth, op->omega);
@@ -669,6 +679,7 @@ agb_status agb_op_create(const int n_cells[3], const double dx[3], const int per
     cudaEventCreate(&op->e1);
     if (!g_attr_done) {
         init_kernel_attributes();
+        init_bottom_attributes();
         g_attr_done = true;
     }
     int dev = 0;
@@ -702,6 +713,10 @@ agb_status agb_op_create(const int n_cells[3], const double dx[3], const int per
     if ((s = op->alloc(&op->d_slots, 16)) != AGB_OK) return bail(s);
     if ((s = op->alloc(&op->bottom_work, 8 * 3 * (size_t)op->lev.back().L.S)) != AGB_OK) return bail(s);
     if ((s = op->alloc(&op->d_ret, 4)) != AGB_OK) return bail(s);
+    if (bottom_dense_fits(op->lev.back().L) && use_dense_bottom()) {
+        if ((s = op->alloc(&op->bottom_A, bottom_dense_bytes(op->lev.back().L) / sizeof(double))) != AGB_OK)
+            return bail(s);
+    }
     op->stage_bytes = 64u << 20;
     if ((s = op->alloc(&op->stage, op->stage_bytes)) != AGB_OK) return bail(s);
     if (cudaMallocHost(&op->h_slots, 16 * sizeof(double)) != cudaSuccess)

@@ -176,6 +176,18 @@ template <typename TD>
 void launch_recip(cudaStream_t st, const LevelDesc& L, int ncomp, const double* d, TD* r);
 void init_kernel_attributes();
 
+// Dense coarsest level (at most 128 unknowns): A assembled once per solve,
+// BiCGStab + smoothing of launch_bottom on it in one warp.
+bool bottom_dense_fits(const LevelDesc& L);
+bool use_dense_bottom();
+size_t bottom_dense_bytes(const LevelDesc& L);
+void launch_bottom_assemble(cudaStream_t st, int sym, const LevelDesc& L, const BCTable& bc, bool uniform,
+                            const double* ddw64, double* A);
+template <typename T>
+void launch_bottom_dense(cudaStream_t st, const LevelDesc& L, const double* A, const double* diag64, T* cor,
+                         const T* res, int maxiter, double tol_rel, double tol_abs, int* ret_slot, int nub, int nuf,
+                         double omega);
+void init_bottom_attributes();
 template <typename T>
 void launch_bottom(cudaStream_t st, int sym, const LevelDesc& L, const BCTable& bc, bool uniform,
                    const double* ddw64, const double* diag64, T* cor, const T* res, double* work, int maxiter,

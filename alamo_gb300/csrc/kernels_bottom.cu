@@ -16,6 +16,8 @@
 // 8 not converged in maxiter.
 #include <cuda_runtime.h>
 
+#include <cstdlib>
+
 #include "agb_internal.h"
 #include "stencil.cuh"
 
@@ -264,6 +266,271 @@ __global__ void __launch_bounds__(BOT_THREADS) k_bottom(LevelDesc L, BCTable bc,
     FOR_NODES(q) cor[q] = (T)sol[q];
     if (threadIdx.x == 0 && ret_slot) *ret_slot = ret;
 }
+
+// ---------------------------------------------------------------------------
+// Dense coarsest level.  When the bottom level has at most DENSE_MAX unknowns
+// (3 x nodes; 81 for the 3^3-node level of a 2^k-cell box) its operator is
+// assembled once per solve as a dense matrix, column j = A e_j evaluated with
+// the same per-node rows (stencil.cuh), and the bottom solve runs the same
+// BiCGStab + smoothing as k_bottom with dense products in one warp: no
+// barrier between warps, and the operator read from shared memory instead of
+// re-evaluating every stencil row.  Results equal k_bottom's up to the
+// summation order of A x.
+// ---------------------------------------------------------------------------
+constexpr int DENSE_MAX = 128;   // unknowns; 4 per lane of one warp
+
+// Unknown q = c * cnt + e, e = i + nn0 * (j + nn1 * k) the node's place in the
+// level's node enumeration.
+__device__ __forceinline__ long long dense_to_padded(const LevelDesc& L, int q, int cnt)
+{
+    const int c = q / cnt, e = q - c * cnt;
+    return c * L.S + L.idx(e % L.nn[0], (e / L.nn[0]) % L.nn[1], e / (L.nn[0] * L.nn[1]));
+}
+
+// Neighbour offsets of node (i,j,k) in the padded layout, periodic wrap included.
+struct UnitAcc {
+    const double* c;
+    long long S, base, unit;   // unit: padded node index of the unit vector's node
+    int comp;                  // and its component
+    long long o[3][3];
+    __device__ __forceinline__ long long off(int di, int dj, int dk) const
+    {
+        return base + o[0][di + 1] + o[1][dj + 1] + o[2][dk + 1];
+    }
+    __device__ __forceinline__ double u(int p, int di, int dj, int dk) const
+    {
+        return (p == comp && off(di, dj, dk) == unit) ? 1.0 : 0.0;
+    }
+    __device__ __forceinline__ double C(int m, int di, int dj, int dk) const { return c[m * S + off(di, dj, dk)]; }
+};
+
+// A (column-major, entry (row r, column j) at j * nu + r) of the level:
+// one thread per (row node, column unknown), rows of its three components.
+template <int SYM>
+__global__ void k_bottom_assemble(LevelDesc L, BCTable bc, Geo<double> g, int uniform,
+                                  const double* __restrict__ ddw, double* __restrict__ A)
+{
+    const int cnt = (int)L.count(), nu = 3 * cnt;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= cnt * nu) return;
+    const int e = t % cnt, col = t / cnt;
+    const int i = e % L.nn[0], j = (e / L.nn[0]) % L.nn[1], k = e / (L.nn[0] * L.nn[1]);
+    const int ce = col % cnt;
+    UnitAcc acc;
+    acc.c = ddw;
+    acc.S = L.S;
+    acc.base = L.idx(i, j, k);
+    acc.comp = col / cnt;
+    acc.unit = L.idx(ce % L.nn[0], (ce / L.nn[0]) % L.nn[1], ce / (L.nn[0] * L.nn[1]));
+    const long long st[3] = {1, (long long)L.P, (long long)L.P * L.nn[1]};
+    const int pos[3] = {i, j, k};
+    int mn[3], mx[3];
+    bool bnd = false;
+    for (int d = 0; d < 3; d++) {
+        mn[d] = !L.per[d] && pos[d] == 0;
+        mx[d] = !L.per[d] && pos[d] == L.n[d];
+        bnd = bnd || mn[d] || mx[d];
+        acc.o[d][0] = -st[d];
+        acc.o[d][1] = 0;
+        acc.o[d][2] = st[d];
+        if (L.per[d]) {
+            if (pos[d] == 0) acc.o[d][0] = st[d] * (L.n[d] - 1);
+            if (pos[d] == L.n[d] - 1) acc.o[d][2] = -st[d] * (L.n[d] - 1);
+        }
+    }
+    double f[3];
+    if (bnd) boundary_row<double, SYM>(acc, g, bc, mn, mx, f);
+    else interior_row<double, SYM>(acc, g, uniform != 0, f);
+    for (int c = 0; c < 3; c++) A[(long long)col * nu + c * cnt + e] = f[c];
+}
+
+// The BiCGStab + smoothing of k_bottom on the dense operator, one thread per
+// unknown (DENSE_MAX threads), arithmetic in R.  The FP64 solve runs it in
+// FP64; the FP32 cycles of the mixed solve run it in FP32, like the rest of
+// their cycle (GB300's FP64 rate per SM sub-partition is about 1/64 of its
+// FP32 rate, so an FP64 bottom solve would cost more than the FP32 cycle
+// around it).
+template <typename R> struct DenseRed {
+    R* red;   // shared, 3 * (DENSE_MAX / 32)
+    __device__ __forceinline__ R sum(R v) const
+    {
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        __syncthreads();
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+        __syncthreads();
+        R t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w];
+        return t;
+    }
+    __device__ __forceinline__ R max(R v) const
+    {
+        for (int o = 16; o > 0; o >>= 1) {
+            const R w = __shfl_xor_sync(0xffffffffu, v, o);
+            v = (w > v || w != w) ? w : v;
+        }
+        __syncthreads();
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+        __syncthreads();
+        R t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t = (red[w] > t || red[w] != red[w]) ? red[w] : t;
+        return t;
+    }
+};
+
+template <typename T, typename R>
+__global__ void __launch_bounds__(DENSE_MAX) k_bottom_dense(LevelDesc L, const double* __restrict__ Ag,
+                                                            const double* __restrict__ diag, T* __restrict__ cor,
+                                                            const T* __restrict__ res, int maxiter, double eps_rel_d,
+                                                            double eps_abs_d, int nub, int nuf, double omega_d,
+                                                            int* ret_slot)
+{
+    extern __shared__ __align__(16) unsigned char dsm_raw[];
+    const int cnt = (int)L.count(), nu = 3 * cnt;
+    R* A = reinterpret_cast<R*>(dsm_raw);
+    R* xs = A + nu * nu;
+    __shared__ R red_s[DENSE_MAX / 32];
+    const DenseRed<R> red{red_s};
+    for (int q = threadIdx.x; q < nu * nu; q += blockDim.x) A[q] = (R)Ag[q];
+    const int q = threadIdx.x;
+    const bool ok = q < nu;
+    const int comp = ok ? q / cnt : 0;
+    const long long pq = ok ? dense_to_padded(L, q, cnt) : 0;
+    const R b = ok ? (R)res[pq] : (R)0;
+    const R d = ok ? (R)diag[pq] : (R)1;
+    const R eps_rel = (R)eps_rel_d, eps_abs = (R)eps_abs_d, omega = (R)omega_d;
+    const bool sing = L.singular();
+    __syncthreads();
+    // y = A x (x staged through shared memory)
+    auto matvec = [&](R x) -> R {
+        __syncthreads();
+        if (ok) xs[q] = x;
+        __syncthreads();
+        R y = 0;
+        if (ok)
+            for (int j = 0; j < nu; j++) y += A[j * nu + q] * xs[j];
+        return y;
+    };
+    // zero-mean projection per component (fully periodic level)
+    auto project = [&](R v) -> R {
+        const R s0 = red.sum(ok && comp == 0 ? v : (R)0);
+        const R s1 = red.sum(ok && comp == 1 ? v : (R)0);
+        const R s2 = red.sum(ok && comp == 2 ? v : (R)0);
+        const R m = comp == 0 ? s0 : (comp == 1 ? s1 : s2);
+        return ok ? v - m / (R)cnt : (R)0;
+    };
+    R sol = 0, r = 0, rh = 0, p = 0, v = 0, s = 0, t = 0;
+    // r = P(b - A*0)/D, P the zero-mean projection on a singular level
+    const R bp = sing ? project(b) : b;
+    if (ok) {
+        r = bp / d;
+        rh = r;
+    }
+    R rnorm = red.max(fabs(r));
+    const R rnorm0 = rnorm;
+    int ret = 0;
+    R rho_1 = 0, alpha = 0, om = 0;
+    if (!(rnorm0 == 0 || rnorm0 < eps_abs)) {
+        for (int iter = 1; iter <= maxiter; iter++) {
+            const R rho = red.sum(rh * r);
+            if (rho == 0) { ret = 1; break; }
+            if (iter == 1) p = r;
+            else {
+                const R beta = (rho / rho_1) * (alpha / om);
+                p = r + beta * (p - om * v);
+            }
+            v = matvec(p);
+            if (sing) v = project(v);
+            v = ok ? v / d : (R)0;
+            const R rhTv = red.sum(rh * v);
+            if (rhTv != 0) alpha = rho / rhTv;
+            else { ret = 2; break; }
+            sol += alpha * p;
+            s = r - alpha * v;
+            rnorm = red.max(fabs(s));
+            if (rnorm < eps_rel * rnorm0 || rnorm < eps_abs) break;
+            t = matvec(s);
+            if (sing) t = project(t);
+            t = ok ? t / d : (R)0;
+            const R tt = red.sum(t * t);
+            const R ts = red.sum(t * s);
+            if (tt != 0) om = ts / tt;
+            else { ret = 3; break; }
+            sol += om * s;
+            r = s - om * t;
+            rnorm = red.max(fabs(r));
+            if (rnorm < eps_rel * rnorm0 || rnorm < eps_abs) break;
+            if (om == 0) { ret = 4; break; }
+            rho_1 = rho;
+        }
+        if (ret == 0 && rnorm > eps_rel * rnorm0 && rnorm > eps_abs) ret = 8;
+        // MLMG::actualBottomSolve: anything but a clean solve discards the correction
+        if (ret != 0 || !(rnorm < rnorm0)) sol = 0;
+    }
+    // post-smoothing: Fsmooth = 2 Jacobi sweeps each
+    const int nsm = 2 * ((ret == 0) ? nub : nuf);
+    for (int sw = 0; sw < nsm; sw++) {
+        const R Ax = matvec(sol);
+        if (ok) {
+            const R Rx = Ax - sol * d;
+            sol = ((R)1 - omega) * sol + omega * (b - Rx) / d;
+        }
+    }
+    if (ok) cor[pq] = (T)sol;
+    if (threadIdx.x == 0 && ret_slot) *ret_slot = ret;
+}
+
+bool bottom_dense_fits(const LevelDesc& L) { return 3 * L.count() <= DENSE_MAX; }
+
+// Small bottom levels use the dense path unless AGB_BOTTOM_DENSE=0.
+bool use_dense_bottom()
+{
+    static bool v = [] {
+        const char* s = getenv("AGB_BOTTOM_DENSE");
+        return !(s && s[0] == '0');
+    }();
+    return v;
+}
+
+size_t bottom_dense_bytes(const LevelDesc& L)
+{
+    const size_t nu = 3 * (size_t)L.count();
+    return nu * nu * sizeof(double);
+}
+
+void launch_bottom_assemble(cudaStream_t st, int sym, const LevelDesc& L, const BCTable& bc, bool uniform,
+                            const double* ddw64, double* A)
+{
+    const Geo<double> g = make_geo<double>(L);
+    const int cnt = (int)L.count(), work = cnt * 3 * cnt;
+    const int blocks = (work + 255) / 256;
+    if (sym == SYM_ISO) k_bottom_assemble<SYM_ISO><<<blocks, 256, 0, st>>>(L, bc, g, uniform ? 1 : 0, ddw64, A);
+    else k_bottom_assemble<SYM_MM><<<blocks, 256, 0, st>>>(L, bc, g, uniform ? 1 : 0, ddw64, A);
+    count_launch();
+}
+
+template <typename T>
+void launch_bottom_dense(cudaStream_t st, const LevelDesc& L, const double* A, const double* diag64, T* cor,
+                         const T* res, int maxiter, double tol_rel, double tol_abs, int* ret_slot, int nub, int nuf,
+                         double omega)
+{
+    const size_t nu = 3 * (size_t)L.count();
+    const size_t smem = (nu * nu + nu) * sizeof(T);
+    k_bottom_dense<T, T><<<1, DENSE_MAX, smem, st>>>(L, A, diag64, cor, res, maxiter, tol_rel, tol_abs, nub, nuf,
+                                                     omega, ret_slot);
+    count_launch();
+}
+
+void init_bottom_attributes()
+{
+    const int smem = (DENSE_MAX * DENSE_MAX + DENSE_MAX) * (int)sizeof(double);
+    cudaFuncSetAttribute(k_bottom_dense<double, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_bottom_dense<float, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+}
+
+template void launch_bottom_dense<double>(cudaStream_t, const LevelDesc&, const double*, const double*, double*,
+                                          const double*, int, double, double, int*, int, int, double);
+template void launch_bottom_dense<float>(cudaStream_t, const LevelDesc&, const double*, const double*, float*,
+                                         const float*, int, double, double, int*, int, int, double);
 
 template <typename T>
 void launch_bottom(cudaStream_t st, int sym, const LevelDesc& L, const BCTable& bc, bool uniform, const double* ddw64,

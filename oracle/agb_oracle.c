@@ -914,7 +914,9 @@ static int bottom_bicgstab(mg_t* m, int l, double* sol, const double* rhs)
         free(buf);
         return 0;
     }
+    int last_iter = 0;
     for (int iter = 1; iter <= m->p->bottom_max_iter; iter++) {
+        last_iter = iter;
         const double rho = dotxy(g, rh, r);
         if (rho == 0) { ret = 1; break; }
         if (iter == 1) {
@@ -945,6 +947,8 @@ static int bottom_bicgstab(mg_t* m, int l, double* sol, const double* rhs)
         rho_1 = rho;
     }
     if (ret == 0 && rnorm > eps_rel * rnorm0 && rnorm > eps_abs) ret = 8;
+    if (m->p->verbose > 1)
+        fprintf(stderr, "oracle bottom: ret %d after %d iterations, |r| %.3e of %.3e\n", ret, last_iter, rnorm, rnorm0);
     if ((ret == 0 || ret == 8) && rnorm < rnorm0) {
         for (long q = 0; q < n3; q++) sol[q] += sorig[q];
     } else {
