@@ -116,6 +116,10 @@ def lib():
         "agb_op_time_sweep": (st, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]),
         "agb_host_alloc": (st, [ctypes.c_size_t, ctypes.POINTER(vp)]),
         "agb_host_free": (st, [vp]),
+        "agb_gen_voronoi_cubic": (st, [ip, ctypes.c_int, dp, dp, vp, vp, ctypes.c_int, vp]),
+        "agb_gen_ellipsoids": (st, [ip, ctypes.c_int, dp, ctypes.c_double, vp, ctypes.c_int, vp]),
+        "agb_gen_sphere": (st, [ip, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                ctypes.c_double, ctypes.c_double, vp, vp, ctypes.c_int, vp]),
         "agb_batch_create": (st, [ctypes.c_int, ip, dp, ip, ctypes.c_int, ctypes.POINTER(AgbSolverParams),
                                   ctypes.POINTER(vp)]),
         "agb_batch_destroy": (st, [vp]),

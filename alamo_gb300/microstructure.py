@@ -7,12 +7,17 @@ stream so that runs are reproducible on any host.
                        an eigenstrain inside it (65^3-node workload)
     voronoi_cubic      cubic-anisotropic polycrystal: Voronoi grains with
                        uniformly random orientations (257^3-node workload)
+    rve_problem        periodic RVE with diffuse ellipsoidal inclusions
+                       (batched-RVE workload)
+    *_device           the same fields evaluated on the GPU from the same
+                       random draws (agb_gen_* in the C ABI)
     cubic              Matrix4<3,MajorMinor>::Cubic(C11, C12, C44, R)
                        (Set/Matrix4_MajorMinor.H:518-547), including its slot
                        aliasing: the stored value of each of the 21 slots is the
                        rotated non-minor-symmetric tensor at the last (p,q,s,t)
                        of the reference's loop that maps to the slot.
 """
+import ctypes
 import itertools
 
 import numpy as np
@@ -127,48 +132,83 @@ def voronoi_grain_ids(n, pts):
 RVE_EDGES = (32, 48, 64, 80, 96)
 
 
-def rve_problem(q, seed=4242, edges=RVE_EDGES, contrast_max=10.0, width=1.5):
-    """Periodic RVE number q of a batch: edge uniform in `edges` cells, 1-8
-    ellipsoidal isotropic inclusions (semi-axes 0.05-0.2 of the edge, random
-    orientation, periodic images) with stiffness contrast log-uniform in
-    [1, contrast_max], matrix lambda = mu = 1, and a macroscopic strain with
-    symmetric entries U(+-1e-3) applied as the uniform eigenstrain F0 = -strain.
-
-    The inclusion boundary is diffuse: log(contrast) follows a tanh profile of
-    `width` cells across the approximate distance to the ellipsoid surface, as
-    a phase-field microstructure would give.  The operator's grad(C) term is a
-    central difference, and a stiffness jump of tens across one cell makes it
-    lose diagonal dominance: the damped-Jacobi multigrid then diverges on the
-    same material with any boundary condition, so sharp inclusions are not a
-    usable workload for this solver.
-    Returns (n, ddw AoS (lambda, mu) on the (n+1)^3 nodal box, F0 (3x3))."""
+def rve_params(q, seed=4242, edges=RVE_EDGES, contrast_max=100.0):
+    """The random draws of periodic RVE number q of a batch: edge uniform in
+    `edges` cells, 1-8 ellipsoidal isotropic inclusions (centre uniform in the
+    cube, semi-axes 0.05-0.2 of the edge, uniformly random orientation,
+    stiffness contrast log-uniform in [1, contrast_max]) in a matrix with
+    lambda = mu = 1, and a macroscopic strain with symmetric entries
+    U(+-1e-3) applied as the uniform eigenstrain F0 = -strain.
+    Returns (n, inclusion table (ninc, 16): centre[3], semi-axes[3], R[9]
+    row-major, log(contrast); F0 (3x3))."""
     rng = SplitMix64(seed * 1000003 + q)
     n = int(edges[min(int(rng.uniform() * len(edges)), len(edges) - 1)])
+    ninc = 1 + min(int(rng.uniform() * 8), 7)
+    table = np.zeros((ninc, 16))
+    for t in range(ninc):
+        table[t, 0:3] = [rng.uniform() for _ in range(3)]
+        table[t, 3:6] = [0.05 + 0.15 * rng.uniform() for _ in range(3)]
+        table[t, 6:15] = quat_to_rot([rng.normal() for _ in range(4)]).reshape(9)
+        table[t, 15] = np.log(contrast_max) * rng.uniform()
+    e = np.zeros((3, 3))
+    for a, b in ((0, 0), (1, 1), (2, 2), (0, 1), (0, 2), (1, 2)):
+        e[a, b] = e[b, a] = (2.0 * rng.uniform() - 1.0) * 1e-3
+    return n, table, -e
+
+
+def ellipsoid_field(n, table, width=2.0):
+    """Host evaluation of the inclusion field: lambda = mu = exp(max_t phi_t *
+    log(contrast_t)), phi = (1 - tanh(s n / w_t))/2 with s = (|y/axes| - 1) *
+    mean(axes) the approximate distance to the surface, y = d R, d the
+    nearest periodic image of node - centre, and w_t = width * max(1,
+    log10(contrast_t)) cells, so that log(stiffness) changes by at most about
+    0.6 per cell.  AoS (lambda, mu) on (n+1)^3 nodes."""
     x = np.arange(n + 1) / n
     Z, Y, X = np.meshgrid(x, x, x, indexing="ij")
     P = np.stack([X, Y, Z], axis=-1).reshape(-1, 3)
     logc = np.zeros(P.shape[0])
-    ninc = 1 + min(int(rng.uniform() * 8), 7)
-    for _ in range(ninc):
-        c = np.array([rng.uniform() for _ in range(3)])
-        axes = np.array([0.05 + 0.15 * rng.uniform() for _ in range(3)])
-        R = quat_to_rot([rng.normal() for _ in range(4)])
-        lk = np.log(contrast_max) * rng.uniform()
+    for t in range(table.shape[0]):
+        c, axes, R, lk = table[t, 0:3], table[t, 3:6], table[t, 6:15].reshape(3, 3), table[t, 15]
         d = P - c
         d -= np.round(d)              # nearest periodic image
         y = d @ R                     # components in the inclusion frame
         r = np.sqrt(np.sum((y / axes) ** 2, axis=1))
-        s = (r - 1.0) * axes.mean()   # approximate distance to the surface
-        phi = 0.5 * (1.0 - np.tanh(s * n / width))
+        s = (r - 1.0) * axes.mean()
+        wq = width * max(1.0, lk / np.log(10.0))   # wider for contrasts above 10
+        phi = 0.5 * (1.0 - np.tanh(s * n / wq))
         logc = np.maximum(logc, phi * lk)
     contrast = np.exp(logc)
     ddw = np.empty((P.shape[0], 2))
     ddw[:, 0] = contrast
     ddw[:, 1] = contrast
-    e = np.zeros((3, 3))
-    for a, b in ((0, 0), (1, 1), (2, 2), (0, 1), (0, 2), (1, 2)):
-        e[a, b] = e[b, a] = (2.0 * rng.uniform() - 1.0) * 1e-3
-    return n, ddw.reshape(-1), -e
+    return ddw.reshape(-1)
+
+
+def rve_problem(q, seed=4242, edges=RVE_EDGES, contrast_max=100.0, width=2.0):
+    """Periodic RVE number q of a batch (rve_params), its field evaluated on the host.
+
+    The inclusion boundary is diffuse: log(contrast) follows a tanh profile of
+    `width` cells across the approximate distance to the ellipsoid surface
+    (the 2-cell profile of the sphere-inclusion workload), as a phase-field
+    microstructure would give.  The operator's grad(C) term is a central
+    difference, and a stiffness jump of tens across one cell makes it lose
+    diagonal dominance: the damped-Jacobi multigrid then diverges on the same
+    material with any boundary condition, so sharp inclusions are not a
+    usable workload for this solver.
+    Returns (n, ddw AoS (lambda, mu) on the (n+1)^3 nodal box, F0 (3x3))."""
+    n, table, F0 = rve_params(q, seed, edges, contrast_max)
+    return n, ellipsoid_field(n, table, width), F0
+
+
+def rve_problem_device(q, seed=4242, edges=RVE_EDGES, contrast_max=100.0, width=2.0, out=None):
+    """rve_problem with the field evaluated on the GPU (agb_gen_ellipsoids).
+    Returns (n, ddw as a CUDA float64 tensor, F0)."""
+    import torch
+    n, table, F0 = rve_params(q, seed, edges, contrast_max)
+    ddw = out if out is not None else torch.empty(2 * (n + 1) ** 3, dtype=torch.float64, device="cuda")
+    _check(_gen().agb_gen_ellipsoids(_cells(n), table.shape[0], _dptr(np.ascontiguousarray(table.reshape(-1))),
+                                     float(width), ctypes.c_void_p(ddw.data_ptr()), 1, None))
+    return n, ddw, F0
 
 
 def voronoi_cubic(n=256, ngrains=64, seed=20260, C11=1.68, C12=1.21, C44=0.75):
@@ -176,3 +216,47 @@ def voronoi_cubic(n=256, ngrains=64, seed=20260, C11=1.68, C12=1.21, C44=0.75):
     pts, table = voronoi_seeds(ngrains, seed, C11, C12, C44)
     ids = voronoi_grain_ids(n, pts)
     return table[ids].reshape(-1), ids, table
+
+
+def voronoi_cubic_device(n=256, ngrains=64, seed=20260, C11=1.68, C12=1.21, C44=0.75):
+    """voronoi_cubic with the per-node field built on the GPU
+    (agb_gen_voronoi_cubic).  Returns (ddw CUDA float64 tensor, ids CUDA
+    int32 tensor, table)."""
+    import torch
+    pts, table = voronoi_seeds(ngrains, seed, C11, C12, C44)
+    N = (n + 1) ** 3
+    ddw = torch.empty(21 * N, dtype=torch.float64, device="cuda")
+    ids = torch.empty(N, dtype=torch.int32, device="cuda")
+    _check(_gen().agb_gen_voronoi_cubic(_cells(n), ngrains, _dptr(np.ascontiguousarray(pts.reshape(-1))),
+                                        _dptr(np.ascontiguousarray(table.reshape(-1))),
+                                        ctypes.c_void_p(ddw.data_ptr()), ctypes.c_void_p(ids.data_ptr()), 1, None))
+    return ddw, ids, table
+
+
+def sphere_inclusion_device(n=64, radius=0.25, lam_m=1.0, mu_m=1.0, lam_i=10.0, mu_i=10.0, eig=1e-3):
+    """sphere_inclusion evaluated on the GPU (agb_gen_sphere): (ddw, F0) CUDA tensors."""
+    import torch
+    N = (n + 1) ** 3
+    ddw = torch.empty(2 * N, dtype=torch.float64, device="cuda")
+    F0 = torch.empty(9 * N, dtype=torch.float64, device="cuda")
+    _check(_gen().agb_gen_sphere(_cells(n), radius, lam_m, mu_m, lam_i, mu_i, eig, ctypes.c_void_p(ddw.data_ptr()),
+                                 ctypes.c_void_p(F0.data_ptr()), 1, None))
+    return ddw, F0
+
+
+def _gen():
+    from ._lib import lib
+    return lib()
+
+
+def _check(st):
+    from ._lib import check
+    check(st)
+
+
+def _cells(n):
+    return (ctypes.c_int * 3)(n, n, n)
+
+
+def _dptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))

@@ -213,6 +213,32 @@ agb_status agb_op_time_sweep(agb_op op, int level, int precision, int mode, int 
 agb_status agb_host_alloc(size_t bytes, void** p);
 agb_status agb_host_free(void* p);
 
+/* Synthetic microstructures evaluated on the GPU (the per-node fields of the
+ * seeded generators; the random draws are made by the caller).  Output is the
+ * AoS nodal field of an n-cell box of the unit cube (node (i,j,k) at
+ * (i/n0, j/n1, k/n2), i fastest, n+1 nodes per direction), host or device
+ * memory per `mem`; the call returns once the field is written.
+ * Reference counterparts: IC/Voronoi.H (its seeds come from glibc rand()),
+ * IC/Ellipse.H, Set/Matrix4_MajorMinor.H:518-556 (Cubic), and the eta mixing
+ * of Integrator/Mechanics.H:249-253. */
+/* Voronoi polycrystal: nearest of `ngrains` seeds (3 doubles each; Euclidean,
+ * not periodic, first seed on ties), 21 MajorMinor doubles per grain from
+ * `table`; ids (optional) receives the grain of every node. */
+agb_status agb_gen_voronoi_cubic(const int n_cells[3], int ngrains, const double* seeds, const double* table,
+                                 double* ddw, int* ids, int mem, void* stream);
+/* Isotropic unit matrix with `ninc` diffuse ellipsoidal inclusions, 16 doubles
+ * each: centre[3], semi-axes[3], rotation R[9] (row-major, inclusion frame
+ * y = d R, d the nearest periodic image of node - centre), log(contrast).
+ * lambda = mu = exp(max over inclusions of phi * log(contrast)), phi =
+ * (1 - tanh(s n0 / w))/2, s = (|y / axes| - 1) * mean(axes), w = width_cells *
+ * max(1, log10(contrast)). */
+agb_status agb_gen_ellipsoids(const int n_cells[3], int ninc, const double* inclusions, double width_cells,
+                              double* ddw, int mem, void* stream);
+/* Centred sphere of radius `radius`: eta = (1 - tanh((r - radius)/(2 dx)))/2,
+ * lambda/mu mixed by eta; F0 (optional, 9 per node) = eig * eta * I. */
+agb_status agb_gen_sphere(const int n_cells[3], double radius, double lam_m, double mu_m, double lam_i, double mu_i,
+                          double eig, double* ddw, double* F0, int mem, void* stream);
+
 /* Allocation-free coarsest-level solve.  No counterpart in the reference: it
  * exists for callers that may not allocate device memory when they need a
  * bottom solve -- a host framework that owns all device memory through its
