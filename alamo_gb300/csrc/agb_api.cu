@@ -680,6 +680,7 @@ agb_status agb_op_create(const int n_cells[3], const double dx[3], const int per
     if (!g_attr_done) {
         init_kernel_attributes();
         init_bottom_attributes();
+        init_tma_attributes();
         g_attr_done = true;
     }
     int dev = 0;
@@ -982,6 +983,8 @@ static agb_status solve_resident(agb_solver s, double tol_rel, double tol_abs, a
         s->p.precision == AGB_PREC_MIXED ? solve_mixed(s, tol_rel, tol_abs, rep) : solve_plain(s, tol_rel, tol_abs, rep);
     // and return the displacement modulo rigid translation: zero mean
     if (L0.singular()) launch_remove_mean<double>(op->st, L0, s->x64, op->d_slots + 8);
+    CK(cudaStreamSynchronize(op->st));
+    if (tma_error_take()) return fail(AGB_CUDA, "a TMA plane copy of the stencil kernel did not complete in time");
     return st;
 }
 
@@ -1192,6 +1195,7 @@ agb_status agb_op_time_sweep(agb_op op, int level, int precision, int mode, int 
     float ms = 0;
     CK(cudaEventElapsedTime(&ms, op->e0, op->e1));
     *ms_per_launch = ms / reps;
+    if (tma_error_take()) return fail(AGB_CUDA, "a TMA plane copy of the stencil kernel did not complete in time");
     return AGB_OK;
 }
 

@@ -175,6 +175,13 @@ void launch_remove_mean(cudaStream_t st, const LevelDesc& L, T* x, double* sums3
 template <typename TD>
 void launch_recip(cudaStream_t st, const LevelDesc& L, int ncomp, const double* d, TD* r);
 void init_kernel_attributes();
+// FP32 interior sweep with TMA plane copies (kernels_tma.cu); false = not launched
+bool use_tma_kernel();
+bool tma_supported(const LevelDesc& L);
+bool launch_stencil_tma(cudaStream_t st, int sym, int mode, const LevelDesc& L, bool uniform, const float* ddw,
+                        const float* x, const float* b, const float* dinv, float* out, float omega, void* norm_slot);
+int tma_error_take();   // 1 if a TMA kernel's bounded wait ran out since the last call
+void init_tma_attributes();
 
 // Dense coarsest level (at most 128 unknowns): A assembled once per solve,
 // BiCGStab + smoothing of launch_bottom on it in one warp.

@@ -561,7 +561,13 @@ static void stencil_dispatch(cudaStream_t st, const LevelDesc& L, const BCTable&
     if (big) {
         // interior by the marching kernel, boundary shell by the per-node kernel
         dim3 blk(MT_X, MT_Y, 1);
-        if (sizeof(T) == 4 && use_pipe_kernel()) {
+        if (sizeof(T) == 4 && use_tma_kernel() && tma_supported(L) &&
+            launch_stencil_tma(st, SYM, MODE, L, uniform, reinterpret_cast<const float*>(ddw),
+                               reinterpret_cast<const float*>(x), reinterpret_cast<const float*>(b),
+                               reinterpret_cast<const float*>(diag), reinterpret_cast<float*>(out), (float)omega,
+                               norm_slot)) {
+            // launched by launch_stencil_tma
+        } else if (sizeof(T) == 4 && use_pipe_kernel()) {
             const size_t smem = sizeof(PipeSmem<T, SYM>);
             dim3 grd((L.n[0] - 1 + MT_X - 1) / MT_X, (L.n[1] - 1 + MT_Y - 1) / MT_Y, (L.n[2] - 1 + PT_Z - 1) / PT_Z);
             k_stencil_pipe<T, SYM, MODE><<<grd, blk, smem, st>>>(L, g, uniform ? 1 : 0, ddw, x, b, diag, out, omega,

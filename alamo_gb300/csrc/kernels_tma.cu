@@ -1,0 +1,392 @@
+// kernels_tma.cu -- FP32 interior stencil sweep with TMA plane copies.
+//
+// Same tile, k-march and per-node arithmetic (stencil.cuh) as the cp.async
+// kernel k_stencil_pipe, but each plane of the 32 x 8 column tile (+1 halo,
+// 36 x 10 elements) is brought into shared memory by two tensor copies
+// (cp.async.bulk.tensor.4d: one box of the 3 displacement components, one
+// box of the 2 or 21 modulus planes) issued by one thread and completed on an
+// mbarrier, so the 256 threads of the CTA spend no instructions on address
+// arithmetic for the copies.  u planes live in a ring of 4 slots, moduli in a
+// ring of 3; fill f brings plane k0-1+f (moduli from f = 1) and completes on
+// barrier f % 4.  Every wait on a barrier is bounded: after a wait runs out
+// the thread stops waiting, the CTA's results are void, *err is set, and
+// thread 0 waits (again bounded) for the copies it issued before returning.
+//
+// Tensor maps (one per array and level, cached by address) describe the
+// padded level layout as a 4-D tensor (i, j, k, component) with strides
+// (P, P nn1, S) elements; the box is (36, 10, 1, ncomp) and starts at
+// i = 32 t, so every copy starts on a 16-byte boundary.
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <cudaTypedefs.h>
+
+#include <cstdint>
+#include <cstdlib>
+#include <map>
+#include <mutex>
+#include <tuple>
+
+#include "agb_internal.h"
+#include "stencil.cuh"
+
+namespace agb {
+
+namespace {
+
+constexpr int TT_X = 32, TT_Y = 8, TT_Z = 32;      // tile and k-chunk
+constexpr int TH_Y = TT_Y + 2, TW = 36;             // halo rows, halo row width (9 x 16 bytes)
+constexpr int TU = 4, TC = 3;                       // ring depths
+
+template <int NCOMP> struct SlotSize {
+    // floats per slot, padded so every slot starts on a 128-byte boundary
+    static constexpr int value = ((NCOMP * TH_Y * TW * 4 + 127) / 128) * 128 / 4;
+};
+
+template <int SYM> struct TmaLayout {
+    static constexpr int NC = NCoef<SYM>::value;
+    static constexpr int USLOT = SlotSize<3>::value;
+    static constexpr int CSLOT = SlotSize<NC>::value;
+    static constexpr int UBYTES = 3 * TH_Y * TW * 4;    // bytes one u box writes
+    static constexpr int CBYTES = NC * TH_Y * TW * 4;   // bytes one modulus box writes
+    static constexpr int C_OFF = TU * USLOT;             // floats
+    static constexpr int BAR_OFF_BYTES = (C_OFF + TC * CSLOT) * 4;
+    static constexpr int SMEM = BAR_OFF_BYTES + TU * 8 + 128;   // + room to align the base to 128 bytes
+};
+
+struct TmaAcc {
+    const float* um;  // u slots of planes k-1, k, k+1
+    const float* uk;
+    const float* up;
+    const float* c0;  // modulus slots of planes k, k+1
+    const float* cp;
+    int tx, ty;
+    float cm[21];     // modulus at (i, j, k-1)
+    __device__ __forceinline__ float u(int p, int di, int dj, int dk) const
+    {
+        const float* s = dk < 0 ? um : (dk > 0 ? up : uk);
+        return s[(p * TH_Y + ty + dj) * TW + tx + di];
+    }
+    __device__ __forceinline__ float C(int m, int di, int dj, int dk) const
+    {
+        if (dk < 0) return cm[m];
+        if (dk > 0) return cp[(m * TH_Y + ty) * TW + tx];
+        return c0[(m * TH_Y + ty + dj) * TW + tx + di];
+    }
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect(uint32_t bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+// Bounded wait for the phase of parity `parity` to complete: false after
+// about 2^31 clock cycles (~1 s at 2 GHz) without completion.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
+{
+    const long long t0 = clock64();
+    while (true) {
+        uint32_t ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (ok) return true;
+        if (clock64() - t0 > (1LL << 31)) return false;
+    }
+}
+
+__device__ __forceinline__ void tma_load4(uint32_t dst, const CUtensorMap* map, int x, int y, int z, int c,
+                                          uint32_t bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+        "[%6];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(c), "r"(bar)
+        : "memory");
+}
+
+template <int SYM, int MODE>
+__global__ void __launch_bounds__(TT_X* TT_Y) k_stencil_tma(LevelDesc L, Geo<float> g, int uniform,
+                                                            const __grid_constant__ CUtensorMap tmx,
+                                                            const __grid_constant__ CUtensorMap tmc,
+                                                            const float* __restrict__ ddw,
+                                                            const float* __restrict__ b,
+                                                            const float* __restrict__ dinv, float* __restrict__ out,
+                                                            float omega, void* norm_slot, int* err)
+{
+    typedef TmaLayout<SYM> Lay;
+    constexpr int NC = Lay::NC;
+    extern __shared__ __align__(128) unsigned char tsm_raw[];
+    float* tsm = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(tsm_raw) + 127) & ~(uintptr_t)127);
+    const uint32_t bar0 = smem_u32(reinterpret_cast<unsigned char*>(tsm) + Lay::BAR_OFF_BYTES);
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + TT_X * ty;
+    const int i0 = 1 + blockIdx.x * TT_X, j0 = 1 + blockIdx.y * TT_Y;
+    const int k0 = 1 + blockIdx.z * TT_Z;
+    const int k1 = min(k0 + TT_Z, L.n[2]);   // exclusive
+    const int i = i0 + tx, j = j0 + ty;
+    const bool mine = (i < L.n[0]) && (j < L.n[1]);
+    const long long S = L.S;
+    const int nfill = k1 - k0 + 2;            // fills 0 .. k1-k0+1 (planes k0-1 .. k1)
+
+    // fill f: u plane k0-1+f -> u slot f%4; moduli plane k0-1+f -> c slot (f-1)%3 (f >= 1); barrier f%4
+    auto issue = [&](int f) {
+        const uint32_t bar = bar0 + 8 * (f % TU);
+        const bool withc = f >= 1;
+        mbar_expect(bar, Lay::UBYTES + (withc ? Lay::CBYTES : 0));
+        const int x0 = i0 - 1, y0 = j0 - 1, z = k0 - 1 + f;
+        tma_load4(smem_u32(tsm + (f % TU) * Lay::USLOT), &tmx, x0, y0, z, 0, bar);
+        if (withc) tma_load4(smem_u32(tsm + Lay::C_OFF + ((f - 1) % TC) * Lay::CSLOT), &tmc, x0, y0, z, 0, bar);
+    };
+
+    if (tid == 0) {
+        for (int s = 0; s < TU; s++) mbar_init(bar0 + 8 * s, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    int issued = 0;   // fills issued so far (thread 0's count; uniform logic)
+    if (tid == 0)
+        for (int f = 0; f < TU && f < nfill; f++) issue(f);
+    issued = min(TU, nfill);
+
+    TmaAcc acc;
+    acc.tx = tx + 1;
+    acc.ty = ty + 1;
+    {
+        const long long p = L.idx(min(i, L.n[0]), min(j, L.n[1]), k0 - 1);
+#pragma unroll
+        for (int m = 0; m < NC; m++) acc.cm[m] = __ldg(ddw + m * S + p);
+    }
+
+    float nrm = 0;
+    int waited = 0;     // fills known complete
+    bool good = true;   // every wait so far completed; after a wait runs out the CTA
+                        // stops waiting, finishes its planes (results are void), and
+                        // thread 0 drains its copies at the end
+    // b and 1/D of the first plane; later planes are fetched one plane ahead
+    float bq[3] = {0, 0, 0}, dq[3] = {0, 0, 0};
+    auto fetch = [&](int k, float* bb, float* dd) {
+        if (!mine || k >= k1) return;
+        const long long q = L.idx(i, j, k);
+        if (MODE != MODE_APPLY)
+#pragma unroll
+            for (int c = 0; c < 3; c++) bb[c] = __ldg(b + c * S + q);
+        if (MODE == MODE_JACOBI)
+#pragma unroll
+            for (int c = 0; c < 3; c++) dd[c] = __ldg(dinv + c * S + q);
+    };
+    fetch(k0, bq, dq);
+    for (int k = k0; k < k1; k++) {
+        const int it = k - k0;
+        const long long q = mine ? L.idx(i, j, k) : 0;
+        float bn[3] = {0, 0, 0}, dn[3] = {0, 0, 0};
+        fetch(k + 1, bn, dn);
+        // planes k-1, k, k+1 = fills it, it+1, it+2
+        for (int f = waited; f <= it + 2 && good; f++) good = mbar_wait(bar0 + 8 * (f % TU), (uint32_t)((f / TU) & 1));
+        if (good) waited = it + 3;
+        acc.um = tsm + (it % TU) * Lay::USLOT;
+        acc.uk = tsm + ((it + 1) % TU) * Lay::USLOT;
+        acc.up = tsm + ((it + 2) % TU) * Lay::USLOT;
+        acc.c0 = tsm + Lay::C_OFF + (it % TC) * Lay::CSLOT;
+        acc.cp = tsm + Lay::C_OFF + ((it + 1) % TC) * Lay::CSLOT;
+        if (mine) {
+            float f[3];
+            interior_row<float, SYM>(acc, g, uniform != 0, f);
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                const long long o = c * S + q;
+                if (MODE == MODE_APPLY) {
+                    out[o] = f[c];
+                } else if (MODE == MODE_RESID) {
+                    const float r = bq[c] - f[c];
+                    out[o] = r;
+                    const float a = fabsf(r);
+                    nrm = (a > nrm || a != a) ? a : nrm;
+                } else {
+                    const float xc = acc.uk[(c * TH_Y + ty + 1) * TW + tx + 1];
+                    out[o] = xc + omega * ((bq[c] - f[c]) * dq[c]);
+                }
+            }
+        }
+#pragma unroll
+        for (int m = 0; m < NC; m++) acc.cm[m] = acc.c0[(m * TH_Y + ty + 1) * TW + tx + 1];
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            bq[c] = bn[c];
+            dq[c] = dn[c];
+        }
+        __syncthreads();
+        // the u slot of plane k-1 and the moduli slot of plane k are free: fill it+4 (plane k+3)
+        // (a thread whose wait ran out issues nothing more: re-arming a barrier
+        // whose phase has not completed is not allowed)
+        if (it + TU < nfill && good) {
+            if (tid == 0) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                issue(it + TU);
+            }
+            issued = it + TU + 1;
+        }
+    }
+    if (!good) {
+        // a wait ran out: report it and wait (bounded) for the copies still in flight
+        if (tid == 0) {
+            atomicExch(err, 1);
+            for (int f = waited; f < issued; f++) mbar_wait(bar0 + 8 * (f % TU), (uint32_t)((f / TU) & 1));
+        }
+        return;
+    }
+    if (MODE == MODE_RESID && norm_slot) {
+        // block max -> slot (same encoding as the other stencil kernels)
+        __shared__ float red[32];
+        for (int o = 16; o > 0; o >>= 1) {
+            const float w = __shfl_xor_sync(0xffffffffu, nrm, o);
+            nrm = (w > nrm || w != w) ? w : nrm;
+        }
+        if ((tid & 31) == 0) red[tid >> 5] = nrm;
+        __syncthreads();
+        if (tid < 32) {
+            float v = tid < (TT_X * TT_Y) / 32 ? red[tid] : 0.0f;
+            for (int o = 16; o > 0; o >>= 1) {
+                const float w = __shfl_xor_sync(0xffffffffu, v, o);
+                v = (w > v || w != w) ? w : v;
+            }
+            if (tid == 0) atomicMax((unsigned int*)norm_slot, __float_as_uint(v));
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// tensor maps
+// ---------------------------------------------------------------------------
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }();
+    return fn;
+}
+
+typedef std::tuple<const void*, int, int, int, long long, int> MapKey;
+std::mutex g_map_mutex;
+std::map<MapKey, CUtensorMap> g_maps;
+
+bool plane_map(const float* base, const LevelDesc& L, int ncomp, CUtensorMap* out)
+{
+    const MapKey key(base, L.P, L.nn[1], L.nn[2], L.S, ncomp);
+    std::lock_guard<std::mutex> lock(g_map_mutex);
+    auto it = g_maps.find(key);
+    if (it != g_maps.end()) {
+        *out = it->second;
+        return true;
+    }
+    PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
+    if (!enc) return false;
+    CUtensorMap m;
+    const cuuint64_t dims[4] = {(cuuint64_t)L.P, (cuuint64_t)L.nn[1], (cuuint64_t)L.nn[2], (cuuint64_t)ncomp};
+    const cuuint64_t strides[3] = {(cuuint64_t)L.P * 4, (cuuint64_t)L.P * L.nn[1] * 4, (cuuint64_t)L.S * 4};
+    const cuuint32_t box[4] = {(cuuint32_t)TW, (cuuint32_t)TH_Y, 1, (cuuint32_t)ncomp};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    const CUresult r = enc(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, (void*)base, dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return false;
+    g_maps[key] = m;
+    *out = m;
+    return true;
+}
+
+__device__ int g_tma_error = 0;
+int* g_tma_error_addr = nullptr;   // device address, looked up at initialisation
+
+}  // namespace
+
+// The TMA kernel serves FP32 interiors unless AGB_STENCIL=pipe or =march.
+bool use_tma_kernel()
+{
+    static bool v = [] {
+        const char* s = getenv("AGB_STENCIL");
+        return !(s && (s[0] == 'p' || s[0] == 'm'));
+    }();
+    return v;
+}
+
+bool tma_supported(const LevelDesc& L)
+{
+    // 16-byte aligned strides; box width inside the padded row (make_level guarantees
+    // P >= last tile start + 36 when x is not periodic)
+    return !L.per[0] && (L.P % 4) == 0 && (L.S % 4) == 0 && encode_fn() != nullptr;
+}
+
+template <int SYM, int MODE>
+static bool launch_tma_sm(cudaStream_t st, const LevelDesc& L, bool uniform, const float* ddw, const float* x,
+                          const float* b, const float* dinv, float* out, float omega, void* norm_slot)
+{
+    CUtensorMap mx, mc;
+    if (!plane_map(x, L, 3, &mx) || !plane_map(ddw, L, NCoef<SYM>::value, &mc)) return false;
+    int* err = g_tma_error_addr;
+    if (!err) return false;
+    const Geo<float> g = make_geo<float>(L);
+    dim3 blk(TT_X, TT_Y, 1);
+    dim3 grd((L.n[0] - 1 + TT_X - 1) / TT_X, (L.n[1] - 1 + TT_Y - 1) / TT_Y, (L.n[2] - 1 + TT_Z - 1) / TT_Z);
+    k_stencil_tma<SYM, MODE><<<grd, blk, TmaLayout<SYM>::SMEM, st>>>(L, g, uniform ? 1 : 0, mx, mc, ddw, b, dinv,
+                                                                     out, omega, norm_slot, err);
+    return true;   // the caller counts the launch
+}
+
+bool launch_stencil_tma(cudaStream_t st, int sym, int mode, const LevelDesc& L, bool uniform, const float* ddw,
+                        const float* x, const float* b, const float* dinv, float* out, float omega, void* norm_slot)
+{
+#define TM(S, M) return launch_tma_sm<S, M>(st, L, uniform, ddw, x, b, dinv, out, omega, norm_slot)
+    if (sym == SYM_ISO) {
+        if (mode == MODE_APPLY) TM(SYM_ISO, MODE_APPLY);
+        if (mode == MODE_RESID) TM(SYM_ISO, MODE_RESID);
+        TM(SYM_ISO, MODE_JACOBI);
+    }
+    if (mode == MODE_APPLY) TM(SYM_MM, MODE_APPLY);
+    if (mode == MODE_RESID) TM(SYM_MM, MODE_RESID);
+    TM(SYM_MM, MODE_JACOBI);
+#undef TM
+}
+
+// Reads and clears the error flag the TMA kernels set when a wait runs out.
+int tma_error_take()
+{
+    int v = 0, z = 0;
+    if (cudaMemcpyFromSymbol(&v, g_tma_error, sizeof(int)) != cudaSuccess) return 0;
+    if (v) cudaMemcpyToSymbol(g_tma_error, &z, sizeof(int));
+    return v;
+}
+
+void init_tma_attributes()
+{
+    if (cudaGetSymbolAddress((void**)&g_tma_error_addr, g_tma_error) != cudaSuccess) g_tma_error_addr = nullptr;
+    cudaFuncSetAttribute(k_stencil_tma<SYM_ISO, MODE_APPLY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         TmaLayout<SYM_ISO>::SMEM);
+    cudaFuncSetAttribute(k_stencil_tma<SYM_ISO, MODE_RESID>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         TmaLayout<SYM_ISO>::SMEM);
+    cudaFuncSetAttribute(k_stencil_tma<SYM_ISO, MODE_JACOBI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         TmaLayout<SYM_ISO>::SMEM);
+    cudaFuncSetAttribute(k_stencil_tma<SYM_MM, MODE_APPLY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         TmaLayout<SYM_MM>::SMEM);
+    cudaFuncSetAttribute(k_stencil_tma<SYM_MM, MODE_RESID>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         TmaLayout<SYM_MM>::SMEM);
+    cudaFuncSetAttribute(k_stencil_tma<SYM_MM, MODE_JACOBI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         TmaLayout<SYM_MM>::SMEM);
+}
+
+}  // namespace agb

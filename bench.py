@@ -367,7 +367,7 @@ def main():
     ms = res["kernels_ms"]["jacobi_f32"]
     achieved = BYTES_PER_NODE["jacobi_f32_cubic"] * nodes / (ms * 1e-3) / 1e9
     traffic = profile_traffic().get("jacobi_f32_cubic_257", {}).get("dram_bytes_per_launch")
-    roof = {"kernel": "k_stencil_pipe<float,MajorMinor,Jacobi> + k_stencil_shell (finest level)",
+    roof = {"kernel": "k_stencil_tma<MajorMinor,Jacobi> + k_stencil_shell (finest level)",
             "bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": peak_kind,
             "bytes_per_launch": BYTES_PER_NODE["jacobi_f32_cubic"] * nodes, "ms_per_launch": ms}
