@@ -116,6 +116,18 @@ def lib():
         "agb_op_time_sweep": (st, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]),
         "agb_host_alloc": (st, [ctypes.c_size_t, ctypes.POINTER(vp)]),
         "agb_host_free": (st, [vp]),
+        "agb_conv3_forward": (st, [ip, ctypes.c_int, ctypes.c_int, vp, vp, vp, vp, ctypes.c_int, ctypes.c_int, vp]),
+        "agb_conv3_wgrad": (st, [ip, ctypes.c_int, ctypes.c_int, vp, vp, vp, vp, vp]),
+        "agb_conv3_flip": (st, [ctypes.c_int, ctypes.c_int, vp, vp, vp]),
+        "agb_relu_backward": (st, [ctypes.c_longlong, vp, vp, vp]),
+        "agb_adam_step": (st, [ctypes.c_longlong, vp, vp, vp, vp, vp, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                               ctypes.c_float, ctypes.c_int, vp]),
+        "agb_learned_create": (st, [ctypes.c_int, ip, ip, ctypes.POINTER(ctypes.c_float),
+                                    ctypes.POINTER(ctypes.c_float), ctypes.POINTER(vp)]),
+        "agb_learned_destroy": (st, [vp]),
+        "agb_learned_features": (st, [ip, vp, vp, ctypes.c_double, vp, vp]),
+        "agb_learned_solve": (st, [vp, vp, vp, vp, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                   ctypes.POINTER(AgbSolveReport)]),
         "agb_gen_voronoi_cubic": (st, [ip, ctypes.c_int, dp, dp, vp, vp, ctypes.c_int, vp]),
         "agb_gen_ellipsoids": (st, [ip, ctypes.c_int, dp, ctypes.c_double, vp, ctypes.c_int, vp]),
         "agb_gen_sphere": (st, [ip, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,

@@ -123,12 +123,25 @@ struct agb_solver_s {
     int g64_fcycle = -1, g32_fcycle = -1;   // cycle kind each graph holds
     long long g64_kernels = 0, g32_kernels = 0;
     long long replayed = 0;                  // kernels executed through graph replays
+    // flexible GCR (agb_learned_solve): stored directions and work vectors
+    std::vector<double*> gZ, gW;
+    double *gr = nullptr, *gz = nullptr, *gw = nullptr, *grv = nullptr, *ge = nullptr, *gt = nullptr;
+    double* gdot = nullptr;
 };
 
 // ---------------------------------------------------------------------------
 // host <-> device field movement
 // ---------------------------------------------------------------------------
 namespace {
+
+// Device fields may still be written by work the caller queued on the legacy
+// default stream (where torch and most callers queue): wait for it before
+// the operator's non-blocking stream touches them.
+agb_status caller_ready(int mem)
+{
+    if (mem == AGB_MEM_DEVICE) CK(cudaStreamSynchronize(cudaStreamLegacy));
+    return AGB_OK;
+}
 
 bool directly_readable(agb_op op, const void* p, int mem)
 {
@@ -146,6 +159,7 @@ template <typename TD, typename TS>
 agb_status upload(agb_op op, const LevelDesc& L, int ncomp, bool aos, const TS* src, int mem, TD* dst)
 {
     if (!src) return fail(AGB_BADARG, "null input field");
+    TRY(caller_ready(mem));
     const int nk = L.n[2] + 1;
     if (directly_readable(op, src, mem)) {
         launch_import<TD, TS>(op->st, L, ncomp, src, dst, aos, 0, L.nn[2], false);
@@ -177,6 +191,7 @@ template <typename TD, typename TS>
 agb_status download(agb_op op, const LevelDesc& L, int ncomp, bool aos, const TS* src, TD* dst, int mem)
 {
     if (!dst) return fail(AGB_BADARG, "null output field");
+    TRY(caller_ready(mem));
     const int nk = L.n[2] + 1;
     if (directly_readable(op, dst, mem)) {
         launch_export<TD, TS>(op->st, L, ncomp, src, dst, aos, 0, nk, false);
@@ -1016,6 +1031,167 @@ agb_status agb_solve(agb_solver s, double* sol, const double* rhs, double tol_re
     if (st != AGB_OK) fail(st, "solve did not converge: status %d after %d iterations, |r| %.3e (target from |r0| %.3e)",
                            (int)st, rep.iterations, rep.res_final, rep.res0);
     return st;
+}
+
+// Flexible GCR with a V-cycle (+ learned correction) preconditioner; see agb.h.
+agb_status agb_learned_solve(agb_solver s, agb_learned net, double* sol, const double* rhs, double tol_rel,
+                             double tol_abs, int restart, int mem, agb_solve_report* report)
+{
+    if (!s || !sol || !rhs) return fail(AGB_BADARG, "null argument");
+    if (restart < 1 || restart > 64) return fail(AGB_BADARG, "restart must be in 1..64");
+    agb_op op = s->op;
+    Level& v0 = op->lev[0];
+    const LevelDesc& L0 = v0.L;
+    if (net && (op->sym != AGB_ISO || !learned_box_ok(L0)))
+        return fail(AGB_BADARG, "the learned correction needs a fully periodic isotropic box with edges "
+                                "multiples of 16, 4 and 2");
+    const size_t n3 = 3 * (size_t)L0.S;
+    while ((int)s->gZ.size() < restart) {
+        double *z = nullptr, *w = nullptr;
+        TRY(op->alloc(&z, n3));
+        TRY(op->alloc(&w, n3));
+        s->gZ.push_back(z);
+        s->gW.push_back(w);
+    }
+    if (!s->gr) {
+        TRY(op->alloc(&s->gr, n3));
+        TRY(op->alloc(&s->gz, n3));
+        TRY(op->alloc(&s->gw, n3));
+        TRY(op->alloc(&s->grv, n3));
+        TRY(op->alloc(&s->ge, n3));
+        TRY(op->alloc(&s->gt, n3));
+        TRY(op->alloc(&s->gdot, 4));
+    }
+    agb_solve_report rep;
+    memset(&rep, 0, sizeof(rep));
+    const long long k0 = launch_counter();
+    cudaStream_t st = op->st;
+    CK(cudaEventRecord(op->e0, st));
+    op->prepared = false;
+    TRY(prepare(op));
+    TRY(ensure_f32(op));
+    TRY((upload<double, double>(op, L0, 3, false, sol, mem, s->x64)));
+    TRY((upload<double, double>(op, L0, 3, false, rhs, mem, s->b64)));
+    const bool sing = L0.singular();
+    if (sing) launch_remove_mean<double>(st, L0, s->b64, op->d_slots + 8);
+    const long long nall = (long long)n3;
+    auto dot = [&](const double* a, const double* b, double* outv) -> agb_status {
+        CK(cudaMemsetAsync(s->gdot, 0, sizeof(double), st));
+        launch_dot(st, nall, a, b, s->gdot);
+        CK(cudaMemcpyAsync(op->h_slots + 12, s->gdot, sizeof(double), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        *outv = op->h_slots[12];
+        return AGB_OK;
+    };
+    auto ninf = [&](const double* a, double* outv) { return norm64(op, L0, a, outv); };
+    Engine<double> E64{op, s->p};
+    Engine<float> E32{op, s->p};
+    // w = P A z (P the zero-mean projection on a fully periodic box)
+    auto apply = [&](const double* z, double* w) {
+        launch_stencil<double>(st, op->sym, MODE_APPLY, L0, op->bc, op->uniform, v0.ddw64, z, nullptr, nullptr, w,
+                               0.0, nullptr);
+        if (sing) launch_remove_mean<double>(st, L0, w, op->d_slots + 11);
+    };
+    // r = b - A x
+    CK(cudaMemsetAsync(op->d_slots, 0, sizeof(double), st));
+    E64.fine_residual(s->x64, s->b64, s->gr, op->d_slots);
+    double res0, bnorm;
+    TRY(ninf(s->gr, &res0));
+    TRY(ninf(s->b64, &bnorm));
+    const double target = std::max(tol_abs, std::max(tol_rel, 1e-16) * std::max(bnorm, res0));
+    rep.res0 = res0;
+    rep.rhs_norm = bnorm;
+    rep.nlevels = (int)op->lev.size();
+    double norm = res0;
+    agb_status status = AGB_MAXITER;
+    int m = 0, fallbacks = 0;
+    if (std::isnan(res0)) status = AGB_NAN;
+    else if (res0 <= target) status = AGB_OK;
+    else {
+        // Add the direction (z, w = P A z) to the GCR space: orthogonalise w
+        // against the stored directions (modified Gram-Schmidt), normalise,
+        // and minimise the residual over the new direction.
+        auto gcr_add = [&](double* z, double* w) -> agb_status {
+            if (m == restart) m = 0;   // restart
+            for (int i = 0; i < m; i++) {
+                double beta;
+                TRY(dot(w, s->gW[i], &beta));
+                launch_axpy<double>(st, L0, 3, w, s->gW[i], -beta);
+                launch_axpy<double>(st, L0, 3, z, s->gZ[i], -beta);
+            }
+            double ww;
+            TRY(dot(w, w, &ww));
+            if (!(ww > 0) || std::isnan(ww)) return std::isnan(ww) ? AGB_NAN : AGB_STALL;
+            const double inv = 1.0 / std::sqrt(ww);
+            launch_zero<double>(st, L0, 3, s->gW[m]);
+            launch_zero<double>(st, L0, 3, s->gZ[m]);
+            launch_axpy<double>(st, L0, 3, s->gW[m], w, inv);
+            launch_axpy<double>(st, L0, 3, s->gZ[m], z, inv);
+            double alpha;
+            TRY(dot(s->gr, s->gW[m], &alpha));
+            launch_axpy<double>(st, L0, 3, s->x64, s->gZ[m], alpha);
+            launch_axpy<double>(st, L0, 3, s->gr, s->gW[m], -alpha);
+            m++;
+            return AGB_OK;
+        };
+        for (int it = 0; it < s->p.max_iter; it++) {
+            // V-cycle direction: z = V(r), one FP32 V-cycle on r / ||r||
+            launch_convert<float, double>(st, L0, 3, s->gr, v0.res32, 1.0 / norm);
+            E32.vcycle(0);
+            launch_zero<double>(st, L0, 3, s->gz);
+            launch_axpy_mixed(st, L0, 3, s->gz, v0.cor32, norm);
+            apply(s->gz, s->gw);
+            agb_status gs = gcr_add(s->gz, s->gw);
+            if (gs != AGB_OK) { status = gs; break; }
+            rep.iterations = it + 1;
+            TRY(ninf(s->gr, &norm));
+            if (s->p.verbose)
+                fprintf(stderr, "agb GCR iter %d V-cycle direction: resid %.6e rel %.6e\n", it + 1, norm,
+                        norm / std::max(bnorm, res0));
+            if (std::isnan(norm)) { status = AGB_NAN; break; }
+            if (norm <= target) { status = AGB_OK; break; }
+            if (!net) continue;
+            // learned direction: e = N(r) on the residual the V-cycle direction left
+            double r2_before, r2_after;
+            TRY(dot(s->gr, s->gr, &r2_before));
+            const agb_status ls = learned_apply(net, st, L0, s->gr, v0.ddw64, s->ge);
+            if (ls != AGB_OK) return fail(ls, "learned correction failed");
+            apply(s->ge, s->gt);
+            gs = gcr_add(s->ge, s->gt);
+            if (gs == AGB_STALL) { fallbacks++; continue; }   // no new direction: the V-cycle carries on
+            if (gs != AGB_OK) { status = gs; break; }
+            TRY(dot(s->gr, s->gr, &r2_after));
+            if (!(r2_after < 0.99 * r2_before)) fallbacks++;   // the learned direction did not help
+            TRY(ninf(s->gr, &norm));
+            if (s->p.verbose)
+                fprintf(stderr, "agb GCR iter %d learned direction: resid %.6e (|r|_2 x %.3f)\n", it + 1, norm,
+                        std::sqrt(r2_after / std::max(r2_before, 1e-300)));
+            if (std::isnan(norm)) { status = AGB_NAN; break; }
+            if (norm <= target) { status = AGB_OK; break; }
+        }
+    }
+    // the true residual of the returned x
+    CK(cudaMemsetAsync(op->d_slots, 0, sizeof(double), st));
+    E64.fine_residual(s->x64, s->b64, s->gr, op->d_slots);
+    TRY(ninf(s->gr, &norm));
+    if (status == AGB_OK && norm > target * 1.0000001) status = AGB_MAXITER;
+    rep.res_final = norm;
+    rep.refinements = fallbacks;
+    if (sing) launch_remove_mean<double>(st, L0, s->x64, op->d_slots + 8);
+    TRY((download<double, double>(op, L0, 3, false, s->x64, sol, mem)));
+    CK(cudaEventRecord(op->e1, st));
+    CK(cudaStreamSynchronize(st));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, op->e0, op->e1);
+    rep.solve_ms = ms;
+    rep.status = status;
+    rep.kernels = launch_counter() - k0;
+    if (report) *report = rep;
+    if (tma_error_take()) return fail(AGB_CUDA, "a TMA plane copy of the stencil kernel did not complete in time");
+    if (status != AGB_OK)
+        fail(status, "GCR did not converge: status %d after %d iterations, |r| %.3e", (int)status, rep.iterations,
+             rep.res_final);
+    return status;
 }
 
 agb_status agb_apply(agb_solver s, double* out, const double* in, int mem)

@@ -524,6 +524,7 @@ agb_status agb_batch_set_model(agb_batch b, int prob, const double* ddw, int lay
     const size_t nfull = (size_t)(L.n[0] + 1) * (L.n[1] + 1) * (L.n[2] + 1) * b->nc;
     const double* src = ddw;
     double* stage = nullptr;
+    if (mem == AGB_MEM_DEVICE) BCK(cudaStreamSynchronize(cudaStreamLegacy));   // the caller's writes of ddw
     if (mem == AGB_MEM_HOST) {
         BCK(cudaMalloc(&stage, nfull * sizeof(double)));
         BCK(cudaMemcpyAsync(stage, ddw, nfull * sizeof(double), cudaMemcpyHostToDevice, b->st));
@@ -706,6 +707,7 @@ agb_status agb_batch_get_solution(agb_batch b, int prob, double* u, int mem)
     const size_t nfull = (size_t)(L.n[0] + 1) * (L.n[1] + 1) * (L.n[2] + 1) * 3;
     double* dst = u;
     double* stage = nullptr;
+    if (mem == AGB_MEM_DEVICE) BCK(cudaStreamSynchronize(cudaStreamLegacy));   // the caller's use of u
     if (mem == AGB_MEM_HOST) {
         BCK(cudaMalloc(&stage, nfull * sizeof(double)));
         dst = stage;

@@ -4,6 +4,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "agb.h"
+
 // Truncated unit normals of BC/Operator/Elastic/Elastic.H:79-80 (kept as the
 // reference writes them: the edge/corner traction rows depend on these digits).
 #define AGB_SQRT3INV 0.57735026919
@@ -168,6 +170,12 @@ template <typename TD, typename TS>
 void launch_export(cudaStream_t st, const LevelDesc& L, int ncomp, const TS* src, TD* dst, bool aos, int k0, int kc,
                    bool chunk);
 void launch_axpy_mixed(cudaStream_t st, const LevelDesc& L, int ncomp, double* y, const float* x, double a);
+// *out += sum x[e] y[e] over n elements (padding entries are zero in every vector)
+void launch_dot(cudaStream_t st, long long n, const double* x, const double* y, double* out);
+// learned correction network (learned.cu)
+bool learned_box_ok(const LevelDesc& L);
+agb_status learned_apply(agb_learned net, cudaStream_t st, const LevelDesc& L, const double* r, const double* ddw64,
+                         double* e);
 // x -= per-component mean over the stored nodes (sums3: 3 doubles of scratch);
 // with norm_slot, also max |x| after the subtraction (atomic max into a zeroed slot)
 template <typename T>

@@ -33,7 +33,7 @@ namespace agb {
 
 namespace {
 
-constexpr int TT_X = 32, TT_Y = 8, TT_Z = 32;      // tile and k-chunk
+constexpr int TT_X = 32, TT_Y = 8, TT_Z = 32;      // tile and the longest k-chunk
 constexpr int TH_Y = TT_Y + 2, TW = 36;             // halo rows, halo row width (9 x 16 bytes)
 constexpr int TU = 4, TC = 3;                       // ring depths
 
@@ -122,7 +122,7 @@ __global__ void __launch_bounds__(TT_X* TT_Y) k_stencil_tma(LevelDesc L, Geo<flo
                                                             const float* __restrict__ ddw,
                                                             const float* __restrict__ b,
                                                             const float* __restrict__ dinv, float* __restrict__ out,
-                                                            float omega, void* norm_slot, int* err)
+                                                            float omega, void* norm_slot, int* err, int kz)
 {
     typedef TmaLayout<SYM> Lay;
     constexpr int NC = Lay::NC;
@@ -131,8 +131,8 @@ __global__ void __launch_bounds__(TT_X* TT_Y) k_stencil_tma(LevelDesc L, Geo<flo
     const uint32_t bar0 = smem_u32(reinterpret_cast<unsigned char*>(tsm) + Lay::BAR_OFF_BYTES);
     const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + TT_X * ty;
     const int i0 = 1 + blockIdx.x * TT_X, j0 = 1 + blockIdx.y * TT_Y;
-    const int k0 = 1 + blockIdx.z * TT_Z;
-    const int k1 = min(k0 + TT_Z, L.n[2]);   // exclusive
+    const int k0 = 1 + blockIdx.z * kz;
+    const int k1 = min(k0 + kz, L.n[2]);   // exclusive
     const int i = i0 + tx, j = j0 + ty;
     const bool mine = (i < L.n[0]) && (j < L.n[1]);
     const long long S = L.S;
@@ -342,9 +342,14 @@ static bool launch_tma_sm(cudaStream_t st, const LevelDesc& L, bool uniform, con
     if (!err) return false;
     const Geo<float> g = make_geo<float>(L);
     dim3 blk(TT_X, TT_Y, 1);
-    dim3 grd((L.n[0] - 1 + TT_X - 1) / TT_X, (L.n[1] - 1 + TT_Y - 1) / TT_Y, (L.n[2] - 1 + TT_Z - 1) / TT_Z);
+    // k-chunk: the longest (least halo re-read) that still gives at least
+    // three waves of 2 CTAs on each of the 152 SMs
+    const int cxy = ((L.n[0] - 1 + TT_X - 1) / TT_X) * ((L.n[1] - 1 + TT_Y - 1) / TT_Y);
+    int kz = TT_Z;
+    while (kz > 8 && (long long)cxy * ((L.n[2] - 1 + kz - 1) / kz) < 3 * 2 * 152) kz /= 2;
+    dim3 grd((L.n[0] - 1 + TT_X - 1) / TT_X, (L.n[1] - 1 + TT_Y - 1) / TT_Y, (L.n[2] - 1 + kz - 1) / kz);
     k_stencil_tma<SYM, MODE><<<grd, blk, TmaLayout<SYM>::SMEM, st>>>(L, g, uniform ? 1 : 0, mx, mc, ddw, b, dinv,
-                                                                     out, omega, norm_slot, err);
+                                                                     out, omega, norm_slot, err, kz);
     return true;   // the caller counts the launch
 }
 

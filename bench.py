@@ -47,8 +47,9 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cycle", default="F", choices=["F", "V"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "rve"],
-                    help="c2: the 257^3 polycrystal (default); rve: batched periodic RVEs")
+    ap.add_argument("--workload", default="c2", choices=["c2", "rve", "learned"],
+                    help="c2: the 257^3 polycrystal (default); rve: batched periodic RVEs; learned: the learned "
+                         "correction trained on 64^3 RVEs and evaluated at 128^3 and 256^3")
     ap.add_argument("--rves", type=int, default=512, help="rve workload: number of RVEs")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "f64"], help="rve workload")
     return ap.parse_args()
@@ -354,6 +355,64 @@ def run_rve(args, dist):
     dist.close()
 
 
+def run_learned(args, dist):
+    """Learned correction (SURVEY configuration C5): train on 64^3 periodic
+    RVEs, evaluate on unseen 128^3 and 256^3 RVEs against plain FP64
+    multigrid, FP32-in-FP64 multigrid and V-cycle GCR (the ablation)."""
+    import numpy as np
+    import torch
+    from alamo_gb300 import microstructure as M
+    from alamo_gb300.elastic import Constant, Elastic, Linear
+    from alamo_gb300.learned import ConvNet, LearnedSolver, train_highpass, training_pairs
+    torch.cuda.set_device(dist.local)
+    t0 = time.perf_counter()
+    pairs = training_pairs(n=64, count=4, seed=4242)
+    net = ConvNet(seed=1)
+    h_hp = train_highpass(net, pairs, 64, steps=300, lr=5e-5)
+    train_s = time.perf_counter() - t0
+    out = {"train": {"samples": len(pairs), "n": 64, "seconds": train_s, "highpass_loss": [h_hp[0], h_hp[-1]]}}
+    for n in (128, 256):
+        _, ddw, F0 = M.rve_problem_device(9001, seed=99, edges=(n,))
+        op = Elastic([n] * 3, None, "isotropic", periodic=(1, 1, 1))
+        op.SetBC(Constant())
+        op.SetModel(ddw)
+        N = (n + 1) ** 3
+        F0n = torch.from_numpy(np.tile(np.asarray(F0).reshape(9), N)).cuda()
+        zero = torch.zeros(3 * N, dtype=torch.float64, device="cuda")
+        rhs = torch.empty(3 * N, dtype=torch.float64, device="cuda")
+        op.NewtonRHS(zero, zero, F0=F0n, out=rhs)
+        row = {}
+        for name, mk in (("mg_f64", lambda: Linear(op, precision=0)), ("mg_mixed", lambda: Linear(op, precision=1)),
+                         ("gcr_v", lambda: LearnedSolver(op, None, restart=16)),
+                         ("gcr_v_learned", lambda: LearnedSolver(op, net, restart=16))):
+            s = mk()
+            best = None
+            for rep in range(2):
+                x = torch.zeros(3 * N, dtype=torch.float64, device="cuda")
+                s.solve(x, rhs, 1e-8, 0.0)
+                r = s.report
+                if best is None or r.solve_ms < best[0]:
+                    best = (r.solve_ms, r.iterations, r.refinements, r.res_final / max(r.rhs_norm, 1e-300))
+            row[name] = {"ms": round(best[0], 2), "iterations": best[1], "rel_res": best[3]}
+            if name == "gcr_v_learned":
+                row[name]["fallbacks"] = best[2]
+            if hasattr(s, "Clear"):
+                s.Clear()
+            else:
+                s.close()
+        row["speedup_learned_vs_f64"] = round(row["mg_f64"]["ms"] / row["gcr_v_learned"]["ms"], 2)
+        out["%d^3" % n] = row
+        op.close()
+    line = {"metric": "learned correction: solve ms at 128^3 / 256^3 periodic RVEs (trained at 64^3)",
+            "value": out["256^3"]["gcr_v_learned"]["ms"] / 1000.0, "unit": "s", "n_gpus": 1, "steps": 2,
+            "warmup": 0, "higher_is_better": False, "dtype": "bf16 net + f32/f64 solve",
+            "data": "synthetic (seeded RVEs)", "config": {"workload": "C5: net trained on 8 samples of 64^3 RVEs"},
+            "learned": out}
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    dist.close()
+
+
 def main():
     args = parse()
     dist = Dist()
@@ -361,6 +420,8 @@ def main():
         return run_reference(args, dist)
     if args.workload == "rve":
         return run_rve(args, dist)
+    if args.workload == "learned":
+        return run_learned(args, dist)
     res, ddw_h, bc = run_ours(args, dist)
     peak, peak_kind = measured_peak_hbm()
     nodes = res["nodes"]

@@ -17,6 +17,9 @@
  *     AGB_MAJORMINOR; or AGB_LAYOUT_SOA (coefficient-major).
  *   - `mem` says whether pointers are host (AGB_MEM_HOST) or device
  *     (AGB_MEM_DEVICE) memory.  Host pointers may be pageable or pinned.
+ *     Device fields are read after the work queued on the legacy default
+ *     stream when the call is made has completed; work the caller queued on
+ *     other streams must be complete before the call.
  *   - One handle is not re-entrant; distinct handles may be used from
  *     distinct host threads.  Each operator owns one CUDA stream; calls
  *     return after their work has completed.
@@ -238,6 +241,61 @@ agb_status agb_gen_ellipsoids(const int n_cells[3], int ninc, const double* incl
  * lambda/mu mixed by eta; F0 (optional, 9 per node) = eig * eta * I. */
 agb_status agb_gen_sphere(const int n_cells[3], double radius, double lam_m, double mu_m, double lam_i, double mu_i,
                           double eig, double* ddw, double* F0, int mem, void* stream);
+
+/* 3x3x3 convolutions of the learned preconditioner (no reference
+ * counterpart).  Fields are channels-last BF16 [voxel][C] over a fully
+ * periodic box of n[0] x n[1] x n[2] voxels (voxel = x + n0 (y + n1 z); edges
+ * multiples of 16, 4 and 2), C a multiple of 16 (unused channels zero).
+ * Weights are BF16 [27][Cout][Cin], tap = (dx+1) + 3 (dy+1) + 9 (dz+1).
+ * Device pointers; work is queued on `stream` and not waited for.
+ *   forward: out[v][co] = act(bias[co] + sum_tap sum_ci in[v+off(tap)][ci] w[tap][co][ci]),
+ *            out FP32 (out_f32) or BF16, act = ReLU if relu.
+ *   wgrad:   dw[tap][co][ci] += sum_v dy[v][co] in[v+off(tap)][ci] (FP32,
+ *            accumulated), db[co] += sum_v dy[v][co] (db may be NULL).
+ *   flip:    wt[26-tap][ci][co] = w[tap][co][ci]; the data gradient of a layer
+ *            is agb_conv3_forward(dy, wt).
+ *   relu_backward: dy[e] = 0 where y[e] <= 0 (BF16, count elements).
+ *   adam_step: Adam on FP32 weights w with gradient g and moments m, v; the
+ *            BF16 copy w_bf16 (may be NULL) is refreshed. */
+agb_status agb_conv3_forward(const int n[3], int cin, int cout, const void* in, const void* w, const float* bias,
+                             void* out, int out_f32, int relu, void* stream);
+agb_status agb_conv3_wgrad(const int n[3], int cin, int cout, const void* in, const void* dy, float* dw, float* db,
+                           void* stream);
+agb_status agb_conv3_flip(int cin, int cout, const void* w, void* wt, void* stream);
+agb_status agb_relu_backward(long long count, const void* y, void* dy, void* stream);
+agb_status agb_adam_step(long long count, float* w, const float* g, float* m, float* v, void* w_bf16, float lr,
+                         float beta1, float beta2, float eps, int step, void* stream);
+
+/* Learned correction inside a flexible GCR solve (no reference counterpart).
+ * The network is a stack of agb_conv3 layers (channels 16/32/48; the first
+ * takes 16 channels, the last gives 16; hidden layers ReLU, the last linear)
+ * applied to the finest level of a fully periodic isotropic box whose edges
+ * are multiples of 16, 4 and 2: features r/s (3), log(lambda)/4, log(mu)/4, zeros
+ * (s = RMS of r); output channels 0-2 times s h^2 are a displacement
+ * correction.  Weights are FP32 on the host, [27][cout][cin] per layer,
+ * stored as BF16 on the device. */
+typedef struct agb_learned_s* agb_learned;
+agb_status agb_learned_create(int nlayers, const int* cin, const int* cout, const float* weights, const float* biases,
+                              agb_learned* out);
+agb_status agb_learned_destroy(agb_learned net);
+/* Network features of a residual in the reference layout (SoA over (n+1)^3
+ * nodes, periodic duplicates ignored) and isotropic AoS moduli, divided by
+ * `scale`: BF16 [n0 n1 n2][16], device pointers, queued on `stream`. */
+agb_status agb_learned_features(const int n_cells[3], const double* r, const double* ddw, double scale, void* feat,
+                                void* stream);
+/* Flexible GCR (restart after `restart` stored directions) on the solver's
+ * operator, to ||b - A x||_inf <= max(tol_abs, tol_rel max(||b||, ||r0||)).
+ * Each iteration adds the direction V(r) (one FP32 V-cycle of the solver's
+ * multigrid settings) and, with a network, the learned direction N(r) on the
+ * residual that step left; GCR minimises the residual over all stored
+ * directions, so a learned direction that does not help costs its work but
+ * not convergence, and the V-cycle directions carry the solve (the
+ * fallback).  net = NULL gives V-cycle GCR, the ablation baseline.  Fully
+ * periodic boxes use the zero-mean projection of agb_solve.
+ * report->iterations counts V-cycle directions; report->refinements counts
+ * learned directions that reduced ||r||_2 by less than 1 %. */
+agb_status agb_learned_solve(agb_solver s, agb_learned net, double* sol, const double* rhs, double tol_rel,
+                             double tol_abs, int restart, int mem, agb_solve_report* report);
 
 /* Allocation-free coarsest-level solve.  No counterpart in the reference: it
  * exists for callers that may not allocate device memory when they need a
