@@ -128,6 +128,8 @@ def lib():
         "agb_learned_features": (st, [ip, vp, vp, ctypes.c_double, vp, vp]),
         "agb_learned_solve": (st, [vp, vp, vp, vp, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
                                    ctypes.POINTER(AgbSolveReport)]),
+        "agb_write_node_plotfile": (st, [ctypes.c_char_p, ctypes.c_int, ctypes.c_double, ip, dp, dp, ctypes.c_int,
+                                         ctypes.POINTER(ctypes.c_char_p), ip, ctypes.POINTER(vp), ctypes.c_int]),
         "agb_gen_voronoi_cubic": (st, [ip, ctypes.c_int, dp, dp, vp, vp, ctypes.c_int, vp]),
         "agb_gen_ellipsoids": (st, [ip, ctypes.c_int, dp, ctypes.c_double, vp, ctypes.c_int, vp]),
         "agb_gen_sphere": (st, [ip, ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,

@@ -216,6 +216,19 @@ agb_status agb_op_time_sweep(agb_op op, int level, int precision, int mode, int 
 agb_status agb_host_alloc(size_t bytes, void** p);
 agb_status agb_host_free(void* p);
 
+/* Nodal plotfile in the AMReX plotfile format, as Integrator::WritePlotFile
+ * writes its nodal fields (Integrator/Integrator.cpp:795-1055) for one level
+ * and one box: <plot_file>/<step, 5 digits>node/{Header, Level_0/Cell_H,
+ * Level_0/Cell_D_00000, Checkpoint}, and the header's name appended to
+ * <plot_file>/nodeoutput.visit (restarted at step 0).  Each field is SoA over
+ * the (n+1)^3 nodes with 1, 3 or 9 components, named like Set::Field
+ * (name; name_x.._z; name_xx, name_xy, .. name_zz row-major); `mem` says
+ * where the fields are.  The box spans prob_lo..prob_hi. */
+agb_status agb_write_node_plotfile(const char* plot_file, int step, double time, const int n_cells[3],
+                                   const double prob_lo[3], const double prob_hi[3], int nfields,
+                                   const char* const* names, const int* ncomp, const double* const* fields,
+                                   int mem);
+
 /* Synthetic microstructures evaluated on the GPU (the per-node fields of the
  * seeded generators; the random draws are made by the caller).  Output is the
  * AoS nodal field of an n-cell box of the unit cube (node (i,j,k) at
