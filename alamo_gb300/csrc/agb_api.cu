@@ -98,6 +98,9 @@ struct agb_op_s {
     int* d_ret = nullptr;
     char* stage = nullptr;       // bounded staging buffer for pageable host copies
     size_t stage_bytes = 0;
+    char* dma = nullptr;         // whole-field staging buffer for pinned host copies (grown on demand)
+    size_t dma_bytes = 0;
+    double *nw_dw = nullptr, *nw_u0 = nullptr, *nw_F0 = nullptr;   // Newton work fields, kept across calls
     int pageable_ok = 0;         // device can read pageable host memory directly
     std::vector<void*> allocs;
 
@@ -143,6 +146,38 @@ agb_status caller_ready(int mem)
     return AGB_OK;
 }
 
+// Pinned host memory: a whole field crosses by one DMA copy (≈ 200 GB/s on
+// GB300) rather than by the import kernel reading host memory (≈ 100 GB/s).
+bool pinned_host(const void* p, int mem)
+{
+    if (mem == AGB_MEM_DEVICE) return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
+agb_status dma_buffer(agb_op op, size_t bytes, char** out)
+{
+    if (bytes > op->dma_bytes) {
+        if (op->dma) {
+            CK(cudaStreamSynchronize(op->st));
+            cudaFree(op->dma);
+            op->dma = nullptr;
+            op->dma_bytes = 0;
+        }
+        if (cudaMalloc(&op->dma, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(AGB_NOMEM, "cudaMalloc(%zu bytes) for the host copy", bytes);
+        }
+        op->dma_bytes = bytes;
+    }
+    *out = op->dma;
+    return AGB_OK;
+}
+
 bool directly_readable(agb_op op, const void* p, int mem)
 {
     if (mem == AGB_MEM_DEVICE) return true;
@@ -161,6 +196,15 @@ agb_status upload(agb_op op, const LevelDesc& L, int ncomp, bool aos, const TS* 
     if (!src) return fail(AGB_BADARG, "null input field");
     TRY(caller_ready(mem));
     const int nk = L.n[2] + 1;
+    if (pinned_host(src, mem)) {
+        const size_t bytes = sizeof(TS) * (size_t)(L.n[0] + 1) * (L.n[1] + 1) * nk * ncomp;
+        char* buf = nullptr;
+        TRY(dma_buffer(op, bytes, &buf));
+        CK(cudaMemcpyAsync(buf, src, bytes, cudaMemcpyHostToDevice, op->st));
+        launch_import<TD, TS>(op->st, L, ncomp, (const TS*)buf, dst, aos, 0, L.nn[2], false);
+        CK(cudaGetLastError());
+        return AGB_OK;
+    }
     if (directly_readable(op, src, mem)) {
         launch_import<TD, TS>(op->st, L, ncomp, src, dst, aos, 0, L.nn[2], false);
         CK(cudaGetLastError());
@@ -193,6 +237,15 @@ agb_status download(agb_op op, const LevelDesc& L, int ncomp, bool aos, const TS
     if (!dst) return fail(AGB_BADARG, "null output field");
     TRY(caller_ready(mem));
     const int nk = L.n[2] + 1;
+    if (pinned_host(dst, mem)) {
+        const size_t bytes = sizeof(TD) * (size_t)(L.n[0] + 1) * (L.n[1] + 1) * nk * ncomp;
+        char* buf = nullptr;
+        TRY(dma_buffer(op, bytes, &buf));
+        launch_export<TD, TS>(op->st, L, ncomp, src, (TD*)buf, aos, 0, nk, false);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(dst, buf, bytes, cudaMemcpyDeviceToHost, op->st));
+        return AGB_OK;
+    }
     if (directly_readable(op, dst, mem)) {
         launch_export<TD, TS>(op->st, L, ncomp, src, dst, aos, 0, nk, false);
         CK(cudaGetLastError());
@@ -747,6 +800,7 @@ agb_status agb_op_destroy(agb_op op)
     if (!op) return AGB_OK;
     if (op->st) cudaStreamSynchronize(op->st);
     for (void* p : op->allocs) cudaFree(p);
+    if (op->dma) cudaFree(op->dma);
     if (op->h_slots) cudaFreeHost(op->h_slots);
     if (op->e0) cudaEventDestroy(op->e0);
     if (op->e1) cudaEventDestroy(op->e1);
@@ -1213,15 +1267,21 @@ agb_status agb_bc_init(agb_op op, double* rhs, int homogeneous, int mem)
     return AGB_OK;
 }
 
+// A finest-level work field kept by the operator across calls (allocated once).
+static agb_status kept(agb_op op, double** slot, size_t count)
+{
+    if (!*slot) TRY(op->alloc(slot, count));
+    return AGB_OK;
+}
+
 static agb_status load_F0(agb_op op, const double* F0, int mem, double** dF0)
 {
     *dF0 = nullptr;
     if (!F0) return AGB_OK;
     Level& v = op->lev[0];
-    double* buf = nullptr;
-    TRY(op->alloc(&buf, 9 * (size_t)v.L.S));
-    TRY((upload<double, double>(op, v.L, 9, true, F0, mem, buf)));
-    *dF0 = buf;
+    TRY(kept(op, &op->nw_F0, 9 * (size_t)v.L.S));
+    TRY((upload<double, double>(op, v.L, 9, true, F0, mem, op->nw_F0)));
+    *dF0 = op->nw_F0;
     return AGB_OK;
 }
 
@@ -1240,7 +1300,8 @@ agb_status agb_newton_rhs(agb_op op, const double* F0, const double* u, const do
     Level& v = op->lev[0];
     double *dF0 = nullptr, *dw = nullptr;
     TRY(load_F0(op, F0, mem, &dF0));
-    agb_status st = op->alloc(&dw, 9 * (size_t)v.L.S);
+    agb_status st = kept(op, &op->nw_dw, 9 * (size_t)v.L.S);
+    dw = op->nw_dw;
     if (st == AGB_OK) st = upload<double, double>(op, v.L, 3, false, u, mem, v.hold64);
     if (st == AGB_OK) st = upload<double, double>(op, v.L, 3, false, b, mem, v.rescor64);
     if (st == AGB_OK) {
@@ -1249,8 +1310,6 @@ agb_status agb_newton_rhs(agb_op op, const double* F0, const double* u, const do
     }
     if (st == AGB_OK) st = download<double, double>(op, v.L, 3, false, v.tmp64, rhs, mem);
     if (st == AGB_OK && cudaStreamSynchronize(op->st) != cudaSuccess) st = fail(AGB_CUDA, "newton rhs failed");
-    release(op, dF0);
-    release(op, dw);
     return st;
 }
 
@@ -1269,8 +1328,10 @@ agb_status agb_newton_solve(agb_solver s, const double* F0, double* u, const dou
     op->prepared = false;   // MLMG::solve -> prepareForSolve on every call
     TRY(prepare(op));
     TRY(load_F0(op, F0, mem, &dF0));
-    agb_status st = op->alloc(&dw, 9 * (size_t)v.L.S);
-    if (st == AGB_OK) st = op->alloc(&u0, 3 * (size_t)v.L.S);
+    agb_status st = kept(op, &op->nw_dw, 9 * (size_t)v.L.S);
+    if (st == AGB_OK) st = kept(op, &op->nw_u0, 3 * (size_t)v.L.S);
+    dw = op->nw_dw;
+    u0 = op->nw_u0;
     if (st == AGB_OK) st = upload<double, double>(op, v.L, 3, false, u, mem, u0);
     if (st == AGB_OK) st = upload<double, double>(op, v.L, 3, false, b, mem, v.rescor64);
     if (st == AGB_OK) {
@@ -1295,9 +1356,6 @@ agb_status agb_newton_solve(agb_solver s, const double* F0, double* u, const dou
         cudaEventElapsedTime(&ms, op->e0, op->e1);
         rep.solve_ms = ms;
     }
-    release(op, dF0);
-    release(op, dw);
-    release(op, u0);
     rep.status = st == AGB_OK ? sst : st;
     rep.kernels = launch_counter() - k0 + s->replayed;
     if (report) *report = rep;
@@ -1318,7 +1376,6 @@ agb_status agb_stress(agb_op op, const double* F0, const double* u, double* sigm
         st = download<double, double>(op, v.L, 9, true, sg, sigma9, mem);
     }
     if (st == AGB_OK && cudaStreamSynchronize(op->st) != cudaSuccess) st = fail(AGB_CUDA, "stress failed");
-    release(op, dF0);
     release(op, sg);
     return st;
 }
@@ -1342,7 +1399,6 @@ agb_status agb_traction_xhi(agb_op op, const double* F0, const double* u, double
         else
             for (int r = 0; r < 3; r++) trac[r] = op->h_slots[4 + r];
     }
-    release(op, dF0);
     release(op, sg);
     return st;
 }
