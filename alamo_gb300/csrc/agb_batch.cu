@@ -54,6 +54,9 @@ struct BLevel {
     int shape = 0;
     std::vector<BTile> tS_smooth, t32_smooth, t32_full;
     BTile *d_tS_smooth = nullptr, *d_t32_smooth = nullptr, *d_t32_full = nullptr;
+    // the same lists restricted to the problems still iterating (compact()),
+    // padded to full length with end markers (prob = -1); the cycle graphs use these
+    BTile *c_tS_smooth = nullptr, *c_t32_smooth = nullptr, *c_t32_full = nullptr;
     std::vector<int> bottoms;
     int* d_bottoms = nullptr;
     long long nvec = 0, ncoef = 0, nwork = 0;
@@ -115,6 +118,8 @@ struct agb_batch_s {
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     cudaGraphExec_t g64 = nullptr, g32 = nullptr;
     long long g64_k = 0, g32_k = 0;
+    long long compact_tiles = -1;   // level-0 tiles in the compacted lists (-1: not built)
+    std::vector<int> compact_mask;
     int grid = 152 * 4;
     bool model_set = false, prepared = false, tuned = false, f0_set = false;
     std::vector<void*> allocs;
@@ -171,10 +176,10 @@ template <typename T> struct BEngine {
         BLevel& v = b->lev[l];
         if (v.tS_smooth.empty()) return;
         for (int s = 0; s < ns; s++) {
-            launch_batch_stencil<T>(b->st, b->sym, MODE_JACOBI, v.shape, b->grid, v.d_probs, v.d_tS_smooth,
+            launch_batch_stencil<T>(b->st, b->sym, MODE_JACOBI, v.shape, b->grid, v.d_probs, v.c_tS_smooth,
                                     (int)v.tS_smooth.size(), act, b->bc, false, A::ddw(v), x, rhs, A::dinv(v), A::tmp(v),
                                     (T)b->omega, nullptr);
-            launch_batch_stencil<T>(b->st, b->sym, MODE_JACOBI, v.shape, b->grid, v.d_probs, v.d_tS_smooth,
+            launch_batch_stencil<T>(b->st, b->sym, MODE_JACOBI, v.shape, b->grid, v.d_probs, v.c_tS_smooth,
                                     (int)v.tS_smooth.size(), act, b->bc, false, A::ddw(v), A::tmp(v), rhs, A::dinv(v), x,
                                     (T)b->omega, nullptr);
         }
@@ -186,19 +191,20 @@ template <typename T> struct BEngine {
         for (int l = 0; l < L; l++) {
             BLevel& v = b->lev[l];
             if (!v.t32_smooth.empty()) {
-                launch_batch_vec(b->st, BV_ZERO, b->grid, v.d_probs, v.d_t32_smooth, (int)v.t32_smooth.size(), act,
+                launch_batch_vec(b->st, BV_ZERO, b->grid, v.d_probs, v.c_t32_smooth, (int)v.t32_smooth.size(), act,
                                  A::cor(v), nullptr, 0.0, nullptr, fp32);
                 smooth(l, A::cor(v), A::res(v), b->p.pre_smooth);
-                launch_batch_stencil<T>(b->st, b->sym, MODE_RESID, v.shape, b->grid, v.d_probs, v.d_tS_smooth,
+                launch_batch_stencil<T>(b->st, b->sym, MODE_RESID, v.shape, b->grid, v.d_probs, v.c_tS_smooth,
                                         (int)v.tS_smooth.size(), act, b->bc, false, A::ddw(v), A::cor(v), A::res(v),
                                         nullptr, A::rescor(v), (T)0, nullptr);
                 BLevel& c = b->lev[l + 1];
-                launch_batch_transfer<T>(b->st, 1, false, b->grid, v.d_probs, c.d_probs, c.d_t32_full,
+                launch_batch_transfer<T>(b->st, 1, false, b->grid, v.d_probs, c.d_probs, c.c_t32_full,
                                          (int)c.t32_full.size(), act, A::rescor(v), A::res(c));
             }
             if (!v.bottoms.empty())
                 launch_batch_bottom(b->st, b->sym, fp32, v.d_probs, v.d_bottoms, (int)v.bottoms.size(), act, b->bc,
-                                    false, v.ddw64, v.diag64, A::cor(v), A::res(v), v.work, b->p.bottom_max_iter,
+                                    false, fp32 ? (const void*)BArr<float>::ddw(v) : (const void*)v.ddw64, v.diag64,
+                                    A::cor(v), A::res(v), v.work, b->p.bottom_max_iter,
                                     b->p.bottom_tol_rel, b->p.bottom_tol_abs, b->p.bottom_smooth, b->p.final_smooth,
                                     b->omega);
         }
@@ -206,7 +212,7 @@ template <typename T> struct BEngine {
             BLevel& v = b->lev[l];
             if (v.t32_smooth.empty()) continue;
             BLevel& c = b->lev[l + 1];
-            launch_batch_transfer<T>(b->st, 0, false, b->grid, v.d_probs, c.d_probs, v.d_t32_smooth,
+            launch_batch_transfer<T>(b->st, 0, false, b->grid, v.d_probs, c.d_probs, v.c_t32_smooth,
                                      (int)v.t32_smooth.size(), act, A::cor(c), A::cor(v));
             smooth(l, A::cor(v), A::res(v), b->p.post_smooth);
         }
@@ -381,7 +387,47 @@ agb_status autotune(agb_batch b)
         make_tiles(v.probs, smooth, dims, v.tS_smooth);
         BTRY(b->upload_vec(v.tS_smooth, &v.d_tS_smooth));
     }
+    for (auto& v : b->lev) {
+        BTRY(b->alloc(&v.c_t32_full, v.t32_full.size()));
+        BTRY(b->alloc(&v.c_t32_smooth, v.t32_smooth.size()));
+        BTRY(b->alloc(&v.c_tS_smooth, v.tS_smooth.size()));
+    }
+    b->compact_tiles = -1;
     b->tuned = true;
+    return AGB_OK;
+}
+
+// Rebuild the compacted tile lists for the problems with mask[q] != 0.  The
+// lists stay supersets of the iterating problems' tiles (the kernels still
+// check the mask), so they are rebuilt only when the level-0 tile count falls
+// by more than 1/16: every skipped tile costs a kernel a dependent load pair.
+agb_status compact(agb_batch b, const std::vector<int>& mask)
+{
+    BLevel& v0 = b->lev[0];
+    long long keep = 0;
+    for (const BTile& t : v0.t32_full) keep += mask[t.prob] != 0;
+    bool subset = b->compact_tiles >= 0 && (int)b->compact_mask.size() == b->np;
+    for (int q = 0; q < b->np && subset; q++) subset = !mask[q] || b->compact_mask[q];
+    if (subset && keep * 16 > b->compact_tiles * 15) return AGB_OK;
+    const BTile end{-1, 0, 0, 0, 0};
+    std::vector<BTile> h;
+    auto put = [&](const std::vector<BTile>& full, BTile* d) -> agb_status {
+        h.clear();
+        for (const BTile& t : full)
+            if (mask[t.prob]) h.push_back(t);
+        h.resize(full.size(), end);
+        if (!h.empty()) BCK(cudaMemcpyAsync(d, h.data(), h.size() * sizeof(BTile), cudaMemcpyHostToDevice, b->st));
+        // h is reused: the copy must finish before the next list is written
+        BCK(cudaStreamSynchronize(b->st));
+        return AGB_OK;
+    };
+    for (auto& v : b->lev) {
+        BTRY(put(v.t32_full, v.c_t32_full));
+        BTRY(put(v.t32_smooth, v.c_t32_smooth));
+        BTRY(put(v.tS_smooth, v.c_tS_smooth));
+    }
+    b->compact_tiles = keep;
+    b->compact_mask = mask;
     return AGB_OK;
 }
 
@@ -392,23 +438,27 @@ agb_status autotune(agb_batch b)
 // projects the right-hand side and every fine residual (and, in the bottom
 // solve, every Krylov residual and operator application), and so finds u with
 // A u = b - c for a uniform body force c of the size of that error.
-template <typename T> void project(agb_batch b, const int* act, T* y, bool norms)
+template <typename T> void project(agb_batch b, const int* act, T* y, bool norms, bool compacted = false)
 {
     BLevel& v = b->lev[0];
+    const BTile* tl = compacted ? v.c_t32_full : v.d_t32_full;
     cudaMemsetAsync(b->sums, 0, sizeof(double) * 3 * b->np, b->st);
-    launch_batch_mean3<T>(b->st, b->grid, v.d_probs, v.d_t32_full, (int)v.t32_full.size(), act, y, b->sums, 0);
-    launch_batch_mean3<T>(b->st, b->grid, v.d_probs, v.d_t32_full, (int)v.t32_full.size(), act, y, b->sums, 1,
+    launch_batch_mean3<T>(b->st, b->grid, v.d_probs, tl, (int)v.t32_full.size(), act, y, b->sums, 0);
+    launch_batch_mean3<T>(b->st, b->grid, v.d_probs, tl, (int)v.t32_full.size(), act, y, b->sums, 1,
                           norms ? (void*)b->d_norms : nullptr);
 }
 
-template <typename T> agb_status residual0(agb_batch b, const int* act, const T* x, const T* rhs, T* r)
+// compacted: use the lists of the problems still iterating (inside the cycle graphs)
+template <typename T>
+agb_status residual0(agb_batch b, const int* act, const T* x, const T* rhs, T* r, bool compacted = false)
 {
     BLevel& v = b->lev[0];
     const bool sing = b->per[0] && b->per[1] && b->per[2];
     BCK(cudaMemsetAsync(b->d_norms, 0, sizeof(double) * b->np, b->st));
-    launch_batch_stencil<T>(b->st, b->sym, MODE_RESID, 0, b->grid, v.d_probs, v.d_t32_full, (int)v.t32_full.size(),
-                            act, b->bc, false, BArr<T>::ddw(v), x, rhs, nullptr, r, (T)0, sing ? nullptr : b->d_norms);
-    if (sing) project<T>(b, act, r, true);
+    launch_batch_stencil<T>(b->st, b->sym, MODE_RESID, 0, b->grid, v.d_probs, compacted ? v.c_t32_full : v.d_t32_full,
+                            (int)v.t32_full.size(), act, b->bc, false, BArr<T>::ddw(v), x, rhs, nullptr, r, (T)0,
+                            sing ? nullptr : b->d_norms);
+    if (sing) project<T>(b, act, r, true, compacted);
     BCK(cudaMemcpyAsync(b->h_norms, b->d_norms, sizeof(double) * b->np, cudaMemcpyDeviceToHost, b->st));
     return AGB_OK;
 }
@@ -586,11 +636,12 @@ agb_status agb_batch_solve(agb_batch b, double tol_rel, double tol_abs, agb_solv
             BTRY(bcapture(b, &b->g64, &b->g64_k, [&] {
                 BEngine<double> E{b, b->d_active};
                 E.vcycle();
-                launch_batch_vec(b->st, BV_AXPY, b->grid, v0.d_probs, v0.d_t32_full, (int)v0.t32_full.size(),
+                launch_batch_vec(b->st, BV_AXPY, b->grid, v0.d_probs, v0.c_t32_full, (int)v0.t32_full.size(),
                                  b->d_active, b->x64, v0.cor64, 1.0, nullptr, 0);
-                residual0<double>(b, b->d_active, b->x64, b->b64, v0.res64);
+                residual0<double>(b, b->d_active, b->x64, b->b64, v0.res64, true);
             }));
         for (int it = 0; it < b->p.max_iter && any(b->active); it++) {
+            BTRY(compact(b, b->active));
             BCK(cudaGraphLaunch(b->g64, b->st));
             replayed += b->g64_k;
             BCK(cudaStreamSynchronize(b->st));
@@ -608,9 +659,9 @@ agb_status agb_batch_solve(agb_batch b, double tol_rel, double tol_abs, agb_solv
             BTRY(bcapture(b, &b->g32, &b->g32_k, [&] {
                 BEngine<float> E{b, b->d_iactive};
                 E.vcycle();
-                launch_batch_vec(b->st, BV_AXPY, b->grid, v0.d_probs, v0.d_t32_full, (int)v0.t32_full.size(),
+                launch_batch_vec(b->st, BV_AXPY, b->grid, v0.d_probs, v0.c_t32_full, (int)v0.t32_full.size(),
                                  b->d_iactive, b->sol32, v0.cor32, 1.0, nullptr, 1);
-                residual0<float>(b, b->d_iactive, b->sol32, b->rhs32, v0.res32);
+                residual0<float>(b, b->d_iactive, b->sol32, b->rhs32, v0.res32, true);
             }));
         std::vector<double> scale(np, 1.0), itol(np);
         for (int outer = 0; outer < b->p.max_refine && any(b->active); outer++) {
@@ -630,6 +681,7 @@ agb_status agb_batch_solve(agb_batch b, double tol_rel, double tol_abs, agb_solv
                              b->sol32, nullptr, 0.0, nullptr, 1);
             std::vector<int> slow(np, 0);
             for (int it = 0; it < b->p.inner_max_iter && any(b->iactive); it++) {
+                BTRY(compact(b, b->iactive));
                 BCK(cudaGraphLaunch(b->g32, b->st));
                 replayed += b->g32_k;
                 BCK(cudaStreamSynchronize(b->st));

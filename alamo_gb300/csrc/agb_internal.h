@@ -119,7 +119,7 @@ void launch_batch_diag(cudaStream_t st, int sym, int grid, const BProb* probs, c
 void launch_batch_vec(cudaStream_t st, int op, int grid, const BProb* probs, const BTile* tiles, int ntiles,
                       const int* active, void* y, const void* x, double a, const double* scale, int fp32);
 void launch_batch_bottom(cudaStream_t st, int sym, int fp32, const BProb* probs, const int* plist, int np,
-                         const int* active, const BCTable& bc, bool uniform, const double* ddw, const double* diag,
+                         const int* active, const BCTable& bc, bool uniform, const void* ddw, const double* diag,
                          void* cor, const void* res, double* work, int maxiter, double tol_rel, double tol_abs, int nub,
                          int nuf, double omega);
 void launch_batch_rhs(cudaStream_t st, int sym, int grid, const BProb* probs, const BTile* tiles, int ntiles,

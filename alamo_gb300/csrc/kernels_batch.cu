@@ -125,14 +125,24 @@ __global__ void __launch_bounds__(256) k_batch_stencil(const BProb* __restrict__
                                                        const T* __restrict__ dinv, T* __restrict__ out, T omega,
                                                        void* norm_slots)
 {
+    // residual norms: each thread keeps its max while the CTA's tiles stay in
+    // one problem (tiles are ordered by problem) and the CTA flushes it to the
+    // problem's slot when the problem changes
+    T nrm = 0;
+    int cur = -1;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const BTile tl = tiles[t];
+        if (tl.prob < 0) break;   // compacted list: only end markers follow (uniform over the CTA)
         if (active && !active[tl.prob]) continue;   // uniform over the CTA
+        if (MODE == MODE_RESID && norm_slots && tl.prob != cur) {
+            if (cur >= 0) tile_max<T>(nrm, norm_slots, cur);
+            nrm = 0;
+            cur = tl.prob;
+        }
         const BProb& P = probs[tl.prob];
         const LevelDesc& L = P.L;
         int i, j, k;
         const bool ok = tile_node<BX, BY, BZ>(tl, L, i, j, k);
-        T nrm = 0;
         if (ok) {
             const Geo<T> g = geo_of<T>(P);
             const T* xp = x + P.vo;
@@ -164,8 +174,8 @@ __global__ void __launch_bounds__(256) k_batch_stencil(const BProb* __restrict__
                 }
             }
         }
-        if (MODE == MODE_RESID && norm_slots) tile_max<T>(nrm, norm_slots, tl.prob);
     }
+    if (MODE == MODE_RESID && norm_slots && cur >= 0) tile_max<T>(nrm, norm_slots, cur);
 }
 
 // Full weighting (restriction) or trilinear prolongation between the levels of
@@ -212,6 +222,7 @@ __global__ void __launch_bounds__(256) k_batch_transfer(int restrict_not_interp,
 {
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const BTile tl = tiles[t];
+        if (tl.prob < 0) break;   // compacted list: only end markers follow (uniform over the CTA)
         if (active && !active[tl.prob]) continue;
         const LevelDesc& Lf = pf[tl.prob].L;
         const LevelDesc& Lc = pc[tl.prob].L;
@@ -329,6 +340,7 @@ __global__ void __launch_bounds__(256) k_batch_vec(int op, const BProb* __restri
 {
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const BTile tl = tiles[t];
+        if (tl.prob < 0) break;   // compacted list: only end markers follow (uniform over the CTA)
         if (active && !active[tl.prob]) continue;
         const BProb& P = probs[tl.prob];
         int i, j, k;
@@ -365,7 +377,7 @@ __global__ void __launch_bounds__(256) k_batch_vec(int op, const BProb* __restri
 // ---------------------------------------------------------------------------
 constexpr int BB_THREADS = 256;
 
-__device__ __forceinline__ double bsum(double v, double* red)
+template <typename R> __device__ __forceinline__ R bsum(R v, R* red)
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -373,7 +385,7 @@ __device__ __forceinline__ double bsum(double v, double* red)
     if (lane == 0) red[warp] = v;
     __syncthreads();
     if (threadIdx.x < 32) {
-        double t = threadIdx.x < (BB_THREADS / 32) ? red[threadIdx.x] : 0.0;
+        R t = threadIdx.x < (BB_THREADS / 32) ? red[threadIdx.x] : (R)0;
         for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
         if (threadIdx.x == 0) red[32] = t;
     }
@@ -381,20 +393,20 @@ __device__ __forceinline__ double bsum(double v, double* red)
     return red[32];
 }
 
-__device__ __forceinline__ double bmax(double v, double* red)
+template <typename R> __device__ __forceinline__ R bmax(R v, R* red)
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int o = 16; o > 0; o >>= 1) {
-        const double w = __shfl_xor_sync(0xffffffffu, v, o);
+        const R w = __shfl_xor_sync(0xffffffffu, v, o);
         v = (w > v || w != w) ? w : v;
     }
     __syncthreads();
     if (lane == 0) red[warp] = v;
     __syncthreads();
     if (threadIdx.x < 32) {
-        double t = threadIdx.x < (BB_THREADS / 32) ? red[threadIdx.x] : 0.0;
+        R t = threadIdx.x < (BB_THREADS / 32) ? red[threadIdx.x] : (R)0;
         for (int o = 16; o > 0; o >>= 1) {
-            const double w = __shfl_xor_sync(0xffffffffu, t, o);
+            const R w = __shfl_xor_sync(0xffffffffu, t, o);
             t = (w > t || w != w) ? w : t;
         }
         if (threadIdx.x == 0) red[32] = t;
@@ -403,16 +415,16 @@ __device__ __forceinline__ double bmax(double v, double* red)
     return red[32];
 }
 
-template <int SYM>
-__device__ void bapply(const BProb& P, const BCTable& bc, int uniform, const double* ddw, const double* x, double* y)
+template <typename R, int SYM>
+__device__ void bapply(const BProb& P, const BCTable& bc, int uniform, const R* ddw, const R* x, R* y)
 {
     const LevelDesc& L = P.L;
-    const Geo<double> g = geo_of<double>(P);
+    const Geo<R> g = geo_of<R>(P);
     const long long cnt = L.count();
     for (long long e = threadIdx.x; e < cnt; e += blockDim.x) {
         const int i = (int)(e % L.nn[0]), j = (int)((e / L.nn[0]) % L.nn[1]),
                   k = (int)(e / ((long long)L.nn[0] * L.nn[1]));
-        BAcc<double> acc{x, ddw, L.S, bnbr(L, i, j, k)};
+        BAcc<R> acc{x, ddw, L.S, bnbr(L, i, j, k)};
         const int pos[3] = {i, j, k};
         int mn[3], mx[3];
         bool bnd = false;
@@ -421,17 +433,17 @@ __device__ void bapply(const BProb& P, const BCTable& bc, int uniform, const dou
             mx[d] = !L.per[d] && pos[d] == L.n[d];
             bnd = bnd || mn[d] || mx[d];
         }
-        double f[3];
-        if (bnd) boundary_row<double, SYM>(acc, g, bc, mn, mx, f);
-        else interior_row<double, SYM>(acc, g, uniform != 0, f);
+        R f[3];
+        if (bnd) boundary_row<R, SYM>(acc, g, bc, mn, mx, f);
+        else interior_row<R, SYM>(acc, g, uniform != 0, f);
         for (int c = 0; c < 3; c++) y[c * L.S + acc.nb.base] = f[c];
     }
 }
 
-__device__ void bmean3(const LevelDesc& L, const double* v, double* red, double m[3])
+template <typename R> __device__ void bmean3(const LevelDesc& L, const R* v, R* red, R m[3])
 {
     const long long cnt = L.count();
-    double s0 = 0, s1 = 0, s2 = 0;
+    R s0 = 0, s1 = 0, s2 = 0;
     for (long long e = threadIdx.x; e < cnt; e += blockDim.x) {
         const long long q = L.idx((int)(e % L.nn[0]), (int)((e / L.nn[0]) % L.nn[1]),
                                   (int)(e / ((long long)L.nn[0] * L.nn[1])));
@@ -439,9 +451,9 @@ __device__ void bmean3(const LevelDesc& L, const double* v, double* red, double 
         s1 += v[L.S + q];
         s2 += v[2 * L.S + q];
     }
-    m[0] = bsum(s0, red) / (double)cnt;
-    m[1] = bsum(s1, red) / (double)cnt;
-    m[2] = bsum(s2, red) / (double)cnt;
+    m[0] = bsum(s0, red) / (R)cnt;
+    m[1] = bsum(s1, red) / (R)cnt;
+    m[2] = bsum(s2, red) / (R)cnt;
 }
 
 #define BFOR(q)                                                                                        \
@@ -454,70 +466,72 @@ __device__ void bmean3(const LevelDesc& L, const double* v, double* red, double 
 template <typename T, int SYM>
 __global__ void __launch_bounds__(BB_THREADS) k_batch_bottom(const BProb* __restrict__ probs, const int* __restrict__ plist,
                                                             const int* __restrict__ active, BCTable bc, int uniform,
-                                                            const double* __restrict__ ddw_all,
+                                                            const T* __restrict__ ddw_all,
                                                             const double* __restrict__ diag_all, T* __restrict__ cor_all,
                                                             const T* __restrict__ res_all, double* __restrict__ work_all,
-                                                            int maxiter, double eps_rel, double eps_abs, int nub, int nuf,
-                                                            double omega)
+                                                            int maxiter, double eps_rel_d, double eps_abs_d, int nub,
+                                                            int nuf, double omega_d)
 {
-    __shared__ double red[33];
+    typedef T R;   // arithmetic in the cycle's precision
+    const R eps_rel = (R)eps_rel_d, eps_abs = (R)eps_abs_d, omega = (R)omega_d;
+    __shared__ R red[33];
     const int pid = plist[blockIdx.x];
     if (active && !active[pid]) return;
     const BProb& P = probs[pid];
     const LevelDesc& L = P.L;
     const long long n3 = 3 * L.S, cnt = L.count();
-    const double* ddw = ddw_all + P.co;
+    const R* ddw = ddw_all + P.co;
     const double* diag = diag_all + P.vo;
     T* cor = cor_all + P.vo;
     const T* res = res_all + P.vo;
-    double* w = work_all + P.wo;
-    double *r = w, *rh = w + n3, *p = w + 2 * n3, *v = w + 3 * n3, *s = w + 4 * n3, *t = w + 5 * n3, *sol = w + 6 * n3,
+    R* w = reinterpret_cast<R*>(work_all + P.wo);
+    R *r = w, *rh = w + n3, *p = w + 2 * n3, *v = w + 3 * n3, *s = w + 4 * n3, *t = w + 5 * n3, *sol = w + 6 * n3,
            *b = w + 7 * n3;
     BFOR(q)
     {
-        b[q] = (double)res[q];
+        b[q] = (R)res[q];
         sol[q] = 0.0;
     }
     __syncthreads();
     const bool sing = L.singular();
-    double mb[3] = {0, 0, 0};
+    R mb[3] = {0, 0, 0};
     if (sing) bmean3(L, b, red, mb);
-    double lm = 0;
+    R lm = 0;
     BFOR(q)
     {
-        r[q] = (b[q] - mb[c_]) / diag[q];
+        r[q] = (b[q] - mb[c_]) / (R)diag[q];
         rh[q] = r[q];
-        const double a = fabs(r[q]);
+        const R a = fabs(r[q]);
         lm = (a > lm || a != a) ? a : lm;
     }
-    double rnorm = bmax(lm, red);
-    const double rnorm0 = rnorm;
+    R rnorm = bmax(lm, red);
+    const R rnorm0 = rnorm;
     int ret = 0;
-    double rho_1 = 0, alpha = 0, om = 0;
+    R rho_1 = 0, alpha = 0, om = 0;
     if (!(rnorm0 == 0 || rnorm0 < eps_abs)) {
         for (int iter = 1; iter <= maxiter; iter++) {
-            double acc = 0;
+            R acc = 0;
             BFOR(q) acc += rh[q] * r[q];
-            const double rho = bsum(acc, red);
+            const R rho = bsum(acc, red);
             if (rho == 0) { ret = 1; break; }
             if (iter == 1) {
                 BFOR(q) p[q] = r[q];
             } else {
-                const double beta = (rho / rho_1) * (alpha / om);
+                const R beta = (rho / rho_1) * (alpha / om);
                 BFOR(q) p[q] = r[q] + beta * (p[q] - om * v[q]);
             }
             __syncthreads();
-            bapply<SYM>(P, bc, uniform, ddw, p, v);
+            bapply<R, SYM>(P, bc, uniform, ddw, p, v);
             __syncthreads();
-            double mv[3] = {0, 0, 0};
+            R mv[3] = {0, 0, 0};
             if (sing) bmean3(L, v, red, mv);
             acc = 0;
             BFOR(q)
             {
-                v[q] = (v[q] - mv[c_]) / diag[q];
+                v[q] = (v[q] - mv[c_]) / (R)diag[q];
                 acc += rh[q] * v[q];
             }
-            const double rhTv = bsum(acc, red);
+            const R rhTv = bsum(acc, red);
             if (rhTv != 0) alpha = rho / rhTv;
             else { ret = 2; break; }
             lm = 0;
@@ -525,19 +539,19 @@ __global__ void __launch_bounds__(BB_THREADS) k_batch_bottom(const BProb* __rest
             {
                 sol[q] += alpha * p[q];
                 s[q] = r[q] - alpha * v[q];
-                const double a = fabs(s[q]);
+                const R a = fabs(s[q]);
                 lm = (a > lm || a != a) ? a : lm;
             }
             rnorm = bmax(lm, red);
             if (rnorm < eps_rel * rnorm0 || rnorm < eps_abs) break;
-            bapply<SYM>(P, bc, uniform, ddw, s, t);
+            bapply<R, SYM>(P, bc, uniform, ddw, s, t);
             __syncthreads();
-            double mt[3] = {0, 0, 0};
+            R mt[3] = {0, 0, 0};
             if (sing) bmean3(L, t, red, mt);
-            double tt = 0, ts = 0;
+            R tt = 0, ts = 0;
             BFOR(q)
             {
-                t[q] = (t[q] - mt[c_]) / diag[q];
+                t[q] = (t[q] - mt[c_]) / (R)diag[q];
                 tt += t[q] * t[q];
                 ts += t[q] * s[q];
             }
@@ -550,7 +564,7 @@ __global__ void __launch_bounds__(BB_THREADS) k_batch_bottom(const BProb* __rest
             {
                 sol[q] += om * s[q];
                 r[q] = s[q] - om * t[q];
-                const double a = fabs(r[q]);
+                const R a = fabs(r[q]);
                 lm = (a > lm || a != a) ? a : lm;
             }
             rnorm = bmax(lm, red);
@@ -566,12 +580,12 @@ __global__ void __launch_bounds__(BB_THREADS) k_batch_bottom(const BProb* __rest
     __syncthreads();
     const int nsm = 2 * ((ret == 0) ? nub : nuf);
     for (int sw = 0; sw < nsm; sw++) {
-        bapply<SYM>(P, bc, uniform, ddw, sol, t);
+        bapply<R, SYM>(P, bc, uniform, ddw, sol, t);
         __syncthreads();
         BFOR(q)
         {
-            const double Rx = t[q] - sol[q] * diag[q];
-            s[q] = (1. - omega) * sol[q] + omega * (b[q] - Rx) / diag[q];
+            const R Rx = t[q] - sol[q] * (R)diag[q];
+            s[q] = ((R)1 - omega) * sol[q] + omega * (b[q] - Rx) / (R)diag[q];
         }
         __syncthreads();
         BFOR(q) sol[q] = s[q];
@@ -663,42 +677,63 @@ __global__ void __launch_bounds__(256) k_batch_mean3(const BProb* __restrict__ p
                                                      int ntiles, const int* __restrict__ active, T* __restrict__ y,
                                                      double* __restrict__ sums, int subtract, void* norm_slots)
 {
+    // A CTA visits tiles t, t + gridDim.x, ...; tiles are ordered by problem, so
+    // consecutive visits mostly stay in one problem.  Each thread accumulates
+    // its sums (or its max |y|) while the problem stays the same, and the CTA
+    // reduces and flushes them with one atomic per value when it changes.
     __shared__ double red[3][8];
+    double s0 = 0, s1 = 0, s2 = 0;
+    T m = 0;
+    int cur = -1;
+    auto flush = [&]() {   // called by every thread of the CTA together
+        if (cur < 0) return;
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        if (subtract) {
+            if (norm_slots) tile_max<T>(m, norm_slots, cur);
+        } else {
+            double v[3] = {s0, s1, s2};
+            for (int c = 0; c < 3; c++) {
+                for (int o = 16; o > 0; o >>= 1) v[c] += __shfl_xor_sync(0xffffffffu, v[c], o);
+                if (lane == 0) red[c][warp] = v[c];
+            }
+            __syncthreads();
+            if (threadIdx.x < 3) {
+                double t = 0;
+                for (int w = 0; w < 8; w++) t += red[threadIdx.x][w];
+                atomicAdd(&sums[cur * 3 + threadIdx.x], t);
+            }
+            __syncthreads();
+        }
+        s0 = s1 = s2 = 0;
+        m = 0;
+    };
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const BTile tl = tiles[t];
+        if (tl.prob < 0) break;   // compacted list: only end markers follow (uniform over the CTA)
         if (active && !active[tl.prob]) continue;   // uniform over the CTA
+        if (tl.prob != cur) {
+            flush();
+            cur = tl.prob;
+        }
         const BProb& P = probs[tl.prob];
         int i, j, k;
-        const bool ok = tile_node<32, 4, 2>(tl, P.L, i, j, k);
-        const long long q = ok ? P.vo + P.L.idx(i, j, k) : 0;
+        if (!tile_node<32, 4, 2>(tl, P.L, i, j, k)) continue;
+        const long long q = P.vo + P.L.idx(i, j, k);
         if (subtract) {
-            T m = 0;
-            if (ok) {
-                const double cnt = (double)P.L.count();
-                for (int c = 0; c < 3; c++) {
-                    const T v = (T)((double)y[q + c * P.L.S] - sums[tl.prob * 3 + c] / cnt);
-                    y[q + c * P.L.S] = v;
-                    const T a = fabs(v);
-                    m = (a > m || a != a) ? a : m;
-                }
+            const double cnt = (double)P.L.count();
+            for (int c = 0; c < 3; c++) {
+                const T v = (T)((double)y[q + c * P.L.S] - sums[tl.prob * 3 + c] / cnt);
+                y[q + c * P.L.S] = v;
+                const T a = fabs(v);
+                m = (a > m || a != a) ? a : m;
             }
-            if (norm_slots) tile_max<T>(m, norm_slots, tl.prob);
-            continue;
+        } else {
+            s0 += (double)y[q];
+            s1 += (double)y[q + P.L.S];
+            s2 += (double)y[q + 2 * P.L.S];
         }
-        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-        for (int c = 0; c < 3; c++) {
-            double v = ok ? (double)y[q + c * P.L.S] : 0.0;
-            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-            if (lane == 0) red[c][warp] = v;
-        }
-        __syncthreads();
-        if (threadIdx.x < 3) {
-            double v = 0;
-            for (int w = 0; w < 8; w++) v += red[threadIdx.x][w];
-            atomicAdd(&sums[tl.prob * 3 + threadIdx.x], v);
-        }
-        __syncthreads();
     }
+    flush();
 }
 
 template <typename T>
@@ -785,13 +820,14 @@ void launch_batch_vec(cudaStream_t st, int op, int grid, const BProb* probs, con
 }
 
 void launch_batch_bottom(cudaStream_t st, int sym, int fp32, const BProb* probs, const int* plist, int np,
-                         const int* active, const BCTable& bc, bool uniform, const double* ddw, const double* diag,
+                         const int* active, const BCTable& bc, bool uniform, const void* ddw, const double* diag,
                          void* cor, const void* res, double* work, int maxiter, double tol_rel, double tol_abs, int nub,
                          int nuf, double omega)
 {
     if (np <= 0) return;
 #define B_(T, S)                                                                                                     \
-    k_batch_bottom<T, S><<<np, BB_THREADS, 0, st>>>(probs, plist, active, bc, uniform ? 1 : 0, ddw, diag, (T*)cor,     \
+    k_batch_bottom<T, S><<<np, BB_THREADS, 0, st>>>(probs, plist, active, bc, uniform ? 1 : 0, (const T*)ddw, diag,  \
+                                                    (T*)cor,                                                           \
                                                     (const T*)res, work, maxiter, tol_rel, tol_abs, nub, nuf, omega)
     if (fp32) {
         if (sym == SYM_ISO) B_(float, SYM_ISO);

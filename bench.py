@@ -317,11 +317,6 @@ def run_rve(args, dist):
     bt.SetEigenstrain(np.stack([p[2] for p in probs]))
     for _ in range(args.warmup):
         bt.solve(1e-8, 0.0, raise_on_fail=False)
-    bad = [q for q in range(nprob) if bt.reports[q].status != 0]
-    for q in bad:
-        r = bt.reports[q]
-        print("rve %d (edge %d): status %d after %d cycles, |r|/|b| %.3e" %
-              (q, probs[q][0], r.status, r.iterations, r.res_final / max(r.rhs_norm, 1e-300)), file=sys.stderr)
     torch.cuda.synchronize()
     dist.barrier()
     clocks = Clocks(dist.local)
@@ -334,6 +329,11 @@ def run_rve(args, dist):
     torch.cuda.synchronize()
     wall = (time.perf_counter() - t0) / args.steps
     clk = clocks.stop()
+    for q in range(nprob):
+        r = bt.reports[q]
+        if r.status != 0:
+            print("rve %d (edge %d): status %d after %d cycles, |r|/|b| %.3e" %
+                  (q, probs[q][0], r.status, r.iterations, r.res_final / max(r.rhs_norm, 1e-300)), file=sys.stderr)
     step_s = dist.max(statistics.mean(ms) / 1000.0)
     its = [bt.reports[q].iterations for q in range(nprob)]
     worst = max(bt.reports[q].res_final / max(bt.reports[q].rhs_norm, 1e-300) for q in range(nprob))
