@@ -15,6 +15,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -351,7 +352,12 @@ agb_status autotune(agb_batch b)
         if (smooth.empty()) continue;
         float best = 1e30f;
         int best_s = 0;
+        // AGB_BATCH_SHAPE=<shape> skips the timing and takes that shape where it serves
+        const char* force = getenv("AGB_BATCH_SHAPE");
+        int forced = force ? atoi(force) : -1;
+        if (!batch_shape_ok(forced, b->sym, b->per)) forced = -1;
         for (int s = 0; s < batch_shape_count(); s++) {
+            if (!batch_shape_ok(s, b->sym, b->per) || (forced >= 0 && s != forced)) continue;
             int dims[3];
             batch_shape_dims(s, dims);
             std::vector<BTile> tl;

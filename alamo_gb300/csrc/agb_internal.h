@@ -134,6 +134,8 @@ void launch_batch_mean3(cudaStream_t st, int grid, const BProb* probs, const BTi
                         const int* active, T* y, double* sums, int subtract, void* norm_slots = nullptr);
 int batch_shape_count();
 void batch_shape_dims(int shape, int dims[3]);
+// whether stencil tile shape `shape` serves batches of this symmetry and periodicity
+bool batch_shape_ok(int shape, int sym, const int per[3]);
 
 // Launchers (kernels_*.cu).  All work is queued on `st`; none synchronizes.
 template <typename T>

@@ -12,16 +12,53 @@
 // (Operator/Elastic.cpp:141-292; transfers Operator.cpp:262-434).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <mutex>
+#include <unordered_map>
+
 #include "agb_internal.h"
 #include "stencil.cuh"
 
 namespace agb {
 
-static const int kShapes[5][3] = {{32, 4, 2}, {32, 8, 1}, {16, 8, 2}, {8, 8, 4}, {64, 4, 1}};
-int batch_shape_count() { return 5; }
+// The persistent launches ask for `grid` CTAs (a few per SM).  A CTA that is
+// not resident from the start runs its share of the tiles after a resident
+// one has finished all of its own, which adds a second wave; so each launch is
+// trimmed to the CTAs of that kernel (256 threads) that fit on the device at
+// once.  Queried once per kernel, outside stream capture (while capturing, an
+// unqueried kernel keeps `grid`).
+static int fit_grid(const void* kernel, int grid, cudaStream_t st)
+{
+    static std::mutex mu;
+    static std::unordered_map<const void*, int> cache;
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find(kernel);
+    if (it != cache.end()) return std::min(grid, it->second);
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return grid;
+    int dev = 0, sms = 0, per = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, 256, 0) != cudaSuccess || per < 1 || sms < 1)
+        return grid;
+    cache[kernel] = sms * per;
+    return std::min(grid, sms * per);
+}
+
+// Shapes 0-4: one node per thread (k_batch_stencil).  Shape 5: 32 x 8 columns
+// marching through 16 planes (k_batch_march), for fully periodic isotropic
+// batches only.
+static const int kShapes[6][3] = {{32, 4, 2}, {32, 8, 1}, {16, 8, 2}, {8, 8, 4}, {64, 4, 1}, {32, 8, 16}};
+constexpr int kMarchShape = 5;
+int batch_shape_count() { return 6; }
 void batch_shape_dims(int shape, int dims[3])
 {
     for (int d = 0; d < 3; d++) dims[d] = kShapes[shape][d];
+}
+bool batch_shape_ok(int shape, int sym, const int per[3])
+{
+    if (shape < 0 || shape >= batch_shape_count()) return false;
+    if (shape == kMarchShape) return sym == SYM_ISO && per[0] && per[1] && per[2];
+    return true;
 }
 
 template <typename T> __device__ __forceinline__ Geo<T> geo_of(const BProb& p)
@@ -173,6 +210,173 @@ __global__ void __launch_bounds__(256) k_batch_stencil(const BProb* __restrict__
                     out[o] = x[o] + omega * ((b[o] - f[c]) * dinv[o]);
                 }
             }
+        }
+    }
+    if (MODE == MODE_RESID && norm_slots && cur >= 0) tile_max<T>(nrm, norm_slots, cur);
+}
+
+// ---------------------------------------------------------------------------
+// Marching tile kernel for fully periodic batches with isotropic moduli.
+//
+// A tile is a 32 x 8 block of columns of one problem and a chunk of up to 16
+// planes.  The CTA walks its chunk plane by plane with the displacement in a
+// shared-memory ring of three haloed planes (k-1, k, k+1) and the moduli in a
+// ring of two (k, k+1); the moduli of the own column at k-1 stay in
+// registers.  The halo wraps periodically (node -1 is node n-1, node n is
+// node 0), so every stored node is an interior node of the stencil.  Each
+// value is read from global memory once per tile instead of once per use,
+// and the loads of plane k+2 are in flight (in registers) while plane k is
+// computed.  The per-node arithmetic is interior_row's, as in k_batch_stencil.
+// ---------------------------------------------------------------------------
+constexpr int BM_X = 32, BM_Y = 8, BM_Z = 16;
+constexpr int BMH_X = BM_X + 2, BMH_Y = BM_Y + 2;
+constexpr int BM_HALO = BMH_X * BMH_Y;                  // 340 halo nodes per plane
+constexpr int BM_PER_THREAD = (BM_HALO + 255) / 256;    // 2 per thread (256 threads)
+
+template <typename T, int SYM> struct BMarchSmem {
+    static constexpr int NC = NCoef<SYM>::value;
+    T u[3][3][BM_HALO];    // [ring slot][component][halo node]
+    T c[2][NC][BM_HALO];
+};
+
+template <typename T, int SYM> struct BMarchAcc {
+    const BMarchSmem<T, SYM>* s;
+    int h;               // halo-tile index of the node
+    int um, u0, up;      // u ring slots of planes k-1, k, k+1
+    int c0, cp;          // moduli ring slots of planes k, k+1
+    T cm[NCoef<SYM>::value];
+    __device__ __forceinline__ T u(int p, int di, int dj, int dk) const
+    {
+        const int r = dk < 0 ? um : (dk > 0 ? up : u0);
+        return s->u[r][p][h + di + BMH_X * dj];
+    }
+    __device__ __forceinline__ T C(int m, int di, int dj, int dk) const
+    {
+        if (dk < 0) return cm[m];
+        if (dk > 0) return s->c[cp][m][h];
+        return s->c[c0][m][h + di + BMH_X * dj];
+    }
+};
+
+__device__ __forceinline__ int pwrap(int i, int n)
+{
+    i %= n;
+    return i < 0 ? i + n : i;
+}
+
+template <typename T, int SYM, int MODE>
+__global__ void __launch_bounds__(256) k_batch_march(const BProb* __restrict__ probs, const BTile* __restrict__ tiles,
+                                                     int ntiles, const int* __restrict__ active, int uniform,
+                                                     const T* __restrict__ ddw, const T* __restrict__ x,
+                                                     const T* __restrict__ b, const T* __restrict__ dinv,
+                                                     T* __restrict__ out, T omega, void* norm_slots)
+{
+    __shared__ __align__(16) BMarchSmem<T, SYM> s;
+    constexpr int NC = NCoef<SYM>::value;
+    const int tid = threadIdx.x, tx = tid % BM_X, ty = tid / BM_X;
+    T nrm = 0;
+    int cur = -1;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const BTile tl = tiles[t];
+        if (tl.prob < 0) break;   // compacted list: only end markers follow (uniform over the CTA)
+        if (active && !active[tl.prob]) continue;
+        if (MODE == MODE_RESID && norm_slots && tl.prob != cur) {
+            if (cur >= 0) tile_max<T>(nrm, norm_slots, cur);
+            nrm = 0;
+            cur = tl.prob;
+        }
+        const BProb& P = probs[tl.prob];
+        const LevelDesc& L = P.L;
+        const Geo<T> g = geo_of<T>(P);
+        const long long S = L.S, plane = (long long)L.P * L.nn[1];
+        const T* xp = x + P.vo;
+        const T* cq = ddw + P.co;
+        const int i0 = tl.bx * BM_X, j0 = tl.by * BM_Y, k0 = tl.bz * BM_Z;
+        const int k1 = min(k0 + BM_Z, L.n[2]);
+        const int i = i0 + tx, j = j0 + ty;
+        const bool mine = i < L.n[0] && j < L.n[1];
+        // in-plane offsets of this thread's halo nodes, wrapped (fixed for the tile)
+        long long hoff[BM_PER_THREAD];
+#pragma unroll
+        for (int q = 0; q < BM_PER_THREAD; q++) {
+            const int e = min(tid + 256 * q, BM_HALO - 1);
+            hoff[q] = (long long)pwrap(i0 - 1 + e % BMH_X, L.n[0]) +
+                      (long long)L.P * pwrap(j0 - 1 + e / BMH_X, L.n[1]);
+        }
+        T ru[BM_PER_THREAD][3], rc[BM_PER_THREAD][NC];
+        auto fetch = [&](int kk) {   // plane kk (wrapped) -> registers
+            const long long pk = plane * pwrap(kk, L.n[2]);
+#pragma unroll
+            for (int q = 0; q < BM_PER_THREAD; q++) {
+                if (tid + 256 * q < BM_HALO) {
+#pragma unroll
+                    for (int c = 0; c < 3; c++) ru[q][c] = __ldg(xp + c * S + hoff[q] + pk);
+#pragma unroll
+                    for (int m = 0; m < NC; m++) rc[q][m] = __ldg(cq + m * S + hoff[q] + pk);
+                }
+            }
+        };
+        auto stash = [&](int ur, int cr, bool with_c) {   // registers -> ring slots
+#pragma unroll
+            for (int q = 0; q < BM_PER_THREAD; q++) {
+                const int e = tid + 256 * q;
+                if (e < BM_HALO) {
+#pragma unroll
+                    for (int c = 0; c < 3; c++) s.u[ur][c][e] = ru[q][c];
+                    if (with_c) {
+#pragma unroll
+                        for (int m = 0; m < NC; m++) s.c[cr][m][e] = rc[q][m];
+                    }
+                }
+            }
+        };
+        BMarchAcc<T, SYM> acc;
+        acc.s = &s;
+        acc.h = (tx + 1) + BMH_X * (ty + 1);
+        acc.um = 0; acc.u0 = 1; acc.up = 2;
+        acc.c0 = 0; acc.cp = 1;
+        {
+            const long long p = (long long)min(i, L.n[0] - 1) + (long long)L.P * min(j, L.n[1] - 1) +
+                                plane * pwrap(k0 - 1, L.n[2]);
+#pragma unroll
+            for (int m = 0; m < NC; m++) acc.cm[m] = __ldg(cq + m * S + p);
+        }
+        fetch(k0 - 1);
+        stash(0, 0, false);
+        fetch(k0);
+        stash(1, 0, true);
+        fetch(k0 + 1);
+        for (int k = k0; k < k1; k++) {
+            stash(acc.up, acc.cp, true);
+            __syncthreads();
+            if (k + 1 < k1) fetch(k + 2);
+            if (mine) {
+                T f[3];
+                interior_row<T, SYM>(acc, g, uniform != 0, f);
+                const long long q0 = P.vo + L.idx(i, j, k);
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    const long long o = q0 + c * S;
+                    if (MODE == MODE_APPLY) out[o] = f[c];
+                    else if (MODE == MODE_RESID) {
+                        const T r = b[o] - f[c];
+                        out[o] = r;
+                        const T a = fabs(r);
+                        nrm = (a > nrm || a != a) ? a : nrm;
+                    } else {
+                        out[o] = s.u[acc.u0][c][acc.h] + omega * ((b[o] - f[c]) * dinv[o]);
+                    }
+                }
+            }
+#pragma unroll
+            for (int m = 0; m < NC; m++) acc.cm[m] = s.c[acc.c0][m][acc.h];
+            __syncthreads();
+            const int r = acc.um;
+            acc.um = acc.u0;
+            acc.u0 = acc.up;
+            acc.up = r;
+            acc.c0 ^= 1;
+            acc.cp ^= 1;
         }
     }
     if (MODE == MODE_RESID && norm_slots && cur >= 0) tile_max<T>(nrm, norm_slots, cur);
@@ -740,6 +944,7 @@ template <typename T>
 void launch_batch_mean3(cudaStream_t st, int grid, const BProb* probs, const BTile* tiles, int ntiles,
                         const int* active, T* y, double* sums, int subtract, void* norm_slots)
 {
+    grid = fit_grid((const void*)k_batch_mean3<T>, grid, st);
     k_batch_mean3<T><<<grid, 256, 0, st>>>(probs, tiles, ntiles, active, y, sums, subtract, norm_slots);
     count_launch();
 }
@@ -757,8 +962,20 @@ static void bst_shape(cudaStream_t st, int shape, int grid, const BProb* probs, 
                       const T* dinv, T* out, T omega, void* norm)
 {
 #define L_(BX, BY, BZ)                                                                                      \
+    grid = fit_grid((const void*)k_batch_stencil<T, SYM, MODE, BX, BY, BZ>, grid, st);                           \
     k_batch_stencil<T, SYM, MODE, BX, BY, BZ><<<grid, 256, 0, st>>>(probs, tiles, ntiles, active, bc, uniform ? 1 : 0, \
                                                                      ddw, x, b, dinv, out, omega, norm)
+    // the marching shape is only chosen for isotropic fully periodic batches
+    // (batch_shape_ok)
+    if constexpr (SYM == SYM_ISO) {
+        if (shape == kMarchShape) {
+            grid = fit_grid((const void*)k_batch_march<T, SYM, MODE>, grid, st);
+            k_batch_march<T, SYM, MODE><<<grid, 256, 0, st>>>(probs, tiles, ntiles, active, uniform ? 1 : 0, ddw, x, b,
+                                                              dinv, out, omega, norm);
+            count_launch();
+            return;
+        }
+    }
     switch (shape) {
     case 0: L_(32, 4, 2); break;
     case 1: L_(32, 8, 1); break;
@@ -792,6 +1009,7 @@ template <typename T>
 void launch_batch_transfer(cudaStream_t st, int restrict_not_interp, bool assign, int grid, const BProb* pf,
                            const BProb* pc, const BTile* tiles, int ntiles, const int* active, const T* src, T* dst)
 {
+    grid = fit_grid((const void*)k_batch_transfer<T>, grid, st);
     k_batch_transfer<T><<<grid, 256, 0, st>>>(restrict_not_interp, assign ? 1 : 0, pf, pc, tiles, ntiles, active, src,
                                               dst);
     count_launch();
@@ -815,6 +1033,7 @@ void launch_batch_diag(cudaStream_t st, int sym, int grid, const BProb* probs, c
 void launch_batch_vec(cudaStream_t st, int op, int grid, const BProb* probs, const BTile* tiles, int ntiles,
                       const int* active, void* y, const void* x, double a, const double* scale, int fp32)
 {
+    grid = fit_grid((const void*)k_batch_vec, grid, st);
     k_batch_vec<<<grid, 256, 0, st>>>(op, probs, tiles, ntiles, active, y, x, a, scale, fp32);
     count_launch();
 }

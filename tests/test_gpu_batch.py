@@ -67,8 +67,41 @@ def test_batch_matches_oracle(gpu_lib, precision):
     s = bt.mean_stress()
     assert np.all(np.isfinite(s)) and np.allclose(s, np.transpose(s, (0, 2, 1)), atol=1e-12)
     for l in range(2):
-        assert bt.tuning(l) in [(32, 4, 2), (32, 8, 1), (16, 8, 2), (8, 8, 4), (64, 4, 1)]
+        assert bt.tuning(l) in [(32, 4, 2), (32, 8, 1), (16, 8, 2), (8, 8, 4), (64, 4, 1), (32, 8, 16)]
     bt.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_batch_march_kernel(gpu_lib, monkeypatch, precision):
+    """The marching tile kernel (32 x 8 columns through 16 planes, fully
+    periodic isotropic batches) forced on every level against the
+    node-per-thread kernel: the same solutions, and within the oracle's
+    tolerance on partial tiles in every direction (edges 40, 24, 12)."""
+    from alamo_gb300.batch import Batch
+    sizes = [40, 24, 12]
+    probs = small_rves(sizes, seed=5)
+    sols, iters = {}, {}
+    for shape, dims in ((0, (32, 4, 2)), (5, (32, 8, 16))):
+        monkeypatch.setenv("AGB_BATCH_SHAPE", str(shape))
+        bt = Batch([(n, n, n) for n in sizes], precision=precision)
+        for q, (n, ddw, F0) in enumerate(probs):
+            bt.SetModel(q, ddw)
+        bt.SetEigenstrain(np.stack([p[2] for p in probs]))
+        assert bt.solve(1e-8, 0.0).status == 0
+        for l in range(2):
+            assert bt.tuning(l) == dims
+        sols[shape] = [bt.solution(q) for q in range(len(sizes))]
+        iters[shape] = [bt.reports[q].iterations for q in range(len(sizes))]
+        bt.close()
+    tol = 1e-10 if precision == 0 else 1e-6
+    for q, (n, ddw, F0) in enumerate(probs):
+        a, b = sols[5][q], sols[0][q]
+        assert np.abs(a - b).max() <= tol * np.abs(b).max(), q
+        assert abs(iters[5][q] - iters[0][q]) <= 1, (q, iters)
+    n, ddw, F0 = probs[0]
+    g, rhs, xo, rep_o = oracle_solution(n, ddw, F0, 1e-8)
+    assert projected_residual_ratio(g, ddw, sols[5][0], rhs, n) <= 1e-8 * 1.00001
+    assert np.abs(sols[5][0] - xo).max() / np.abs(xo).max() < 1e-6
 
 
 def test_single_box_periodic_matches_oracle(gpu_lib):
