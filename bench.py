@@ -270,7 +270,7 @@ def run_ours(args, dist):
         torch.cuda.synchronize()
         parts.clear()
         t0 = time.perf_counter()
-        ke = 2
+        ke = 3
         for _ in range(ke):
             e2e_step()
         e2e_s = dist.max((time.perf_counter() - t0) / ke)
