@@ -21,6 +21,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/agb.h"
@@ -348,6 +349,8 @@ template <> struct Arr<double> {
     static double* tmp(Level& l) { return l.tmp64; }
     static const double* ddw(Level& l) { return l.ddw64; }
     static const double* dinv(Level& l) { return l.dinv64; }
+    static void swap_res_rescor(Level& l) { std::swap(l.res64, l.rescor64); }
+    static void swap_cor_hold(Level& l) { std::swap(l.cor64, l.hold64); }
 };
 template <> struct Arr<float> {
     static float* cor(Level& l) { return l.cor32; }
@@ -357,6 +360,8 @@ template <> struct Arr<float> {
     static float* tmp(Level& l) { return l.tmp32; }
     static const float* ddw(Level& l) { return l.ddw32; }
     static const float* dinv(Level& l) { return l.dinv32; }
+    static void swap_res_rescor(Level& l) { std::swap(l.res32, l.rescor32); }
+    static void swap_cor_hold(Level& l) { std::swap(l.cor32, l.hold32); }
 };
 
 template <typename T> struct Engine {
@@ -437,13 +442,20 @@ template <typename T> struct Engine {
         bottom();
         for (int l = b - 1; l >= 0; l--) {
             Level& v = lv(l);
-            const size_t bytes = sizeof(T) * 3 * (size_t)v.L.S;
             launch_interpolation<T>(op->st, v.L, lv(l + 1).L, A::cor(v), A::cor(lv(l + 1)), true);
             residual(l, A::cor(v), A::res(v), A::rescor(v), nullptr);
-            cudaMemcpyAsync(A::res(v), A::rescor(v), bytes, cudaMemcpyDeviceToDevice, op->st);
-            cudaMemcpyAsync(A::hold(v), A::cor(v), bytes, cudaMemcpyDeviceToDevice, op->st);
+            // The V-cycle's right-hand side is the residual of the interpolated
+            // correction, and the interpolated correction is kept aside: swap
+            // the buffers' roles instead of copying (res <-> rescor, cor <->
+            // hold), add the V-cycle's correction into the kept one, and swap
+            // back, so that cor holds the sum and every buffer has its role
+            // again when the step ends (the captured graph replays from there).
+            A::swap_res_rescor(v);
+            A::swap_cor_hold(v);
             vcycle(l);
-            launch_axpy<T>(op->st, v.L, 3, A::cor(v), A::hold(v), (T)1);
+            launch_axpy<T>(op->st, v.L, 3, A::hold(v), A::cor(v), (T)1);
+            A::swap_res_rescor(v);
+            A::swap_cor_hold(v);
         }
     }
     void cycle(int iter)

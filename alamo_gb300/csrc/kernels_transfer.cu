@@ -53,6 +53,25 @@ __device__ __forceinline__ T full_weight(const F& f, bool bI, bool bJ, bool bK)
            f(0, 0, 0) * (T)(1.0 / 8.0);
 }
 
+// Fine-level offsets of the nodes 2I-1, 2I, 2I+1 (periodic wrap) in the three
+// directions of a coarse node, computed once per thread: each of the 27
+// reads of a full weighting is then one add of three offsets.
+struct FineOffsets {
+    int ox[3];
+    int oy[3];
+    long long oz[3];
+    __device__ __forceinline__ FineOffsets(const LevelDesc& Lf, int I, int J, int K)
+    {
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            ox[a] = wrapn(2 * I + a - 1, Lf.n[0], Lf.per[0]);
+            oy[a] = Lf.P * wrapn(2 * J + a - 1, Lf.n[1], Lf.per[1]);
+            oz[a] = (long long)Lf.P * Lf.nn[1] * wrapn(2 * K + a - 1, Lf.n[2], Lf.per[2]);
+        }
+    }
+    __device__ __forceinline__ long long at(int a, int b, int d) const { return ox[a + 1] + oy[b + 1] + oz[d + 1]; }
+};
+
 template <typename T>
 __global__ void k_restrict(LevelDesc Lf, LevelDesc Lc, const T* __restrict__ fine, T* __restrict__ crse, int ncomp)
 {
@@ -64,44 +83,80 @@ __global__ void k_restrict(LevelDesc Lf, LevelDesc Lc, const T* __restrict__ fin
     const bool bJ = !Lc.per[1] && (J == 0 || J == Lc.n[1]);
     const bool bK = !Lc.per[2] && (K == 0 || K == Lc.n[2]);
     const long long q = Lc.idx(I, J, K);
+    const FineOffsets o(Lf, I, J, K);
     for (int c = 0; c < ncomp; c++) {
         const T* src = fine + c * Lf.S;
-        auto f = [&](int a, int b, int d) -> T {
-            return __ldg(src + Lf.idx(wrapn(2 * I + a, Lf.n[0], Lf.per[0]), wrapn(2 * J + b, Lf.n[1], Lf.per[1]),
-                                      wrapn(2 * K + d, Lf.n[2], Lf.per[2])));
-        };
+        auto f = [&](int a, int b, int d) -> T { return __ldg(src + o.at(a, b, d)); };
         crse[c * Lc.S + q] = full_weight<T>(f, bI, bJ, bK);
     }
 }
 
+template <typename T> struct Pair;
+template <> struct Pair<float> { typedef float2 type; };
+template <> struct Pair<double> { typedef double2 type; };
+
+// Trilinear prolongation of the coarse correction.  A thread owns the fine
+// pair i = 2I, 2I+1 of one row (the even node takes the coarse value at I,
+// the odd one the mean with I+1), so a warp never splits on the parity of i;
+// the parities of j and k are uniform over a warp (one row per warp).  The
+// pair is read and written as one 8- or 16-byte vector (rows start on
+// 32-byte boundaries and 2I is even).  Each fine value is the same
+// expression, summed in the same order, as the per-node form
+// (Operator.cpp:365-434).
 template <typename T>
 __global__ void k_interp(LevelDesc Lf, LevelDesc Lc, T* __restrict__ fine, const T* __restrict__ crse, int assign)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int I = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    const int i = 2 * I;
     if (i >= Lf.nn[0] || j >= Lf.nn[1] || k >= Lf.nn[2]) return;
-    const int I = i >> 1, J = j >> 1, K = k >> 1;
+    const bool two = i + 1 < Lf.nn[0];
+    const int J = j >> 1, K = k >> 1;
     const int I1 = wrapn(I + 1, Lc.n[0], Lc.per[0]), J1 = wrapn(J + 1, Lc.n[1], Lc.per[1]),
               K1 = wrapn(K + 1, Lc.n[2], Lc.per[2]);
-    const bool ei = !(i & 1), ej = !(j & 1), ek = !(k & 1);
+    const bool ej = !(j & 1), ek = !(k & 1);
     const long long q = Lf.idx(i, j, k);
+    const long long r00 = Lc.idx(0, J, K), r10 = Lc.idx(0, J1, K), r01 = Lc.idx(0, J, K1), r11 = Lc.idx(0, J1, K1);
     for (int c = 0; c < 3; c++) {
         const T* cs = crse + c * Lc.S;
-        auto C = [&](int a, int b, int d) -> T { return __ldg(cs + Lc.idx(a ? I1 : I, b ? J1 : J, d ? K1 : K)); };
-        T t;
-        if (ei && ej && ek) t = C(0, 0, 0);
-        else if (ej && ek) t = (T)0.5 * (C(0, 0, 0) + C(1, 0, 0));
-        else if (ek && ei) t = (T)0.5 * (C(0, 0, 0) + C(0, 1, 0));
-        else if (ei && ej) t = (T)0.5 * (C(0, 0, 0) + C(0, 0, 1));
-        else if (ei) t = (T)0.25 * (C(0, 0, 0) + C(0, 1, 0) + C(0, 0, 1) + C(0, 1, 1));
-        else if (ej) t = (T)0.25 * (C(0, 0, 0) + C(0, 0, 1) + C(1, 0, 0) + C(1, 0, 1));
-        else if (ek) t = (T)0.25 * (C(0, 0, 0) + C(1, 0, 0) + C(0, 1, 0) + C(1, 1, 0));
-        else
-            t = (T)0.125 * (C(0, 0, 0) + C(1, 0, 0) + C(0, 1, 0) + C(0, 0, 1) + C(0, 1, 1) + C(1, 0, 1) +
-                            C(1, 1, 0) + C(1, 1, 1));
+        // C(a, b, d): coarse value at (a ? I1 : I, b ? J1 : J, d ? K1 : K)
+        auto C = [&](int a, int b, int d) -> T {
+            const long long r = b ? (d ? r11 : r10) : (d ? r01 : r00);
+            return __ldg(cs + r + (a ? I1 : I));
+        };
+        T te, to = (T)0;
+        if (ej && ek) {
+            te = C(0, 0, 0);
+            if (two) to = (T)0.5 * (C(0, 0, 0) + C(1, 0, 0));
+        } else if (ek) {
+            te = (T)0.5 * (C(0, 0, 0) + C(0, 1, 0));
+            if (two) to = (T)0.25 * (C(0, 0, 0) + C(1, 0, 0) + C(0, 1, 0) + C(1, 1, 0));
+        } else if (ej) {
+            te = (T)0.5 * (C(0, 0, 0) + C(0, 0, 1));
+            if (two) to = (T)0.25 * (C(0, 0, 0) + C(0, 0, 1) + C(1, 0, 0) + C(1, 0, 1));
+        } else {
+            te = (T)0.25 * (C(0, 0, 0) + C(0, 1, 0) + C(0, 0, 1) + C(0, 1, 1));
+            if (two)
+                to = (T)0.125 * (C(0, 0, 0) + C(1, 0, 0) + C(0, 1, 0) + C(0, 0, 1) + C(0, 1, 1) + C(1, 0, 1) +
+                                 C(1, 1, 0) + C(1, 1, 1));
+        }
         T* o = fine + c * Lf.S + q;
-        *o = assign ? t : (*o + t);
+        if (two) {
+            typedef typename Pair<T>::type V;
+            V v;
+            if (assign) {
+                v.x = te;
+                v.y = to;
+            } else {
+                v = *reinterpret_cast<const V*>(o);
+                v.x = v.x + te;
+                v.y = v.y + to;
+            }
+            *reinterpret_cast<V*>(o) = v;
+        } else {
+            *o = assign ? te : (*o + te);
+        }
     }
 }
 
@@ -277,7 +332,10 @@ void launch_interpolation(cudaStream_t st, const LevelDesc& Lf, const LevelDesc&
                           bool assign)
 {
     dim3 blk(32, 4, 2);
-    k_interp<T><<<grid_for(Lf, blk), blk, 0, st>>>(Lf, Lc, fine, crse, assign ? 1 : 0); count_launch();
+    // one thread per fine pair (2I, 2I+1) of a row
+    const dim3 grd(((Lf.nn[0] + 1) / 2 + blk.x - 1) / blk.x, (Lf.nn[1] + blk.y - 1) / blk.y,
+                   (Lf.nn[2] + blk.z - 1) / blk.z);
+    k_interp<T><<<grd, blk, 0, st>>>(Lf, Lc, fine, crse, assign ? 1 : 0); count_launch();
 }
 
 template <typename T>
