@@ -18,6 +18,7 @@
 
 #include "agb_internal.h"
 #include "stencil.cuh"
+#include "transfer.cuh"
 
 namespace agb {
 
@@ -73,35 +74,11 @@ template <typename T> __device__ __forceinline__ Geo<T> geo_of(const BProb& p)
     return g;
 }
 
-struct BNbr {
-    long long base;
-    long long o[3][3];
-};
-
-__device__ __forceinline__ BNbr bnbr(const LevelDesc& L, int i, int j, int k)
-{
-    BNbr nb;
-    nb.base = L.idx(i, j, k);
-    const long long st[3] = {1, (long long)L.P, (long long)L.P * L.nn[1]};
-    const int pos[3] = {i, j, k};
-#pragma unroll
-    for (int d = 0; d < 3; d++) {
-        nb.o[d][0] = -st[d];
-        nb.o[d][1] = 0;
-        nb.o[d][2] = st[d];
-        if (L.per[d]) {
-            if (pos[d] == 0) nb.o[d][0] = st[d] * (L.n[d] - 1);
-            if (pos[d] == L.n[d] - 1) nb.o[d][2] = -st[d] * (L.n[d] - 1);
-        }
-    }
-    return nb;
-}
-
 template <typename T> struct BAcc {
     const T* __restrict__ x;
     const T* __restrict__ c;
     long long S;
-    BNbr nb;
+    Nbr nb;
     __device__ __forceinline__ long long off(int di, int dj, int dk) const
     {
         return nb.base + nb.o[0][di + 1] + nb.o[1][dj + 1] + nb.o[2][dk + 1];
@@ -183,7 +160,7 @@ __global__ void __launch_bounds__(256) k_batch_stencil(const BProb* __restrict__
         if (ok) {
             const Geo<T> g = geo_of<T>(P);
             const T* xp = x + P.vo;
-            BAcc<T> acc{xp, ddw + P.co, L.S, bnbr(L, i, j, k)};
+            BAcc<T> acc{xp, ddw + P.co, L.S, make_nbr(L, i, j, k)};
             const int pos[3] = {i, j, k};
             int mn[3], mx[3];
             bool bnd = false;
@@ -384,39 +361,6 @@ __global__ void __launch_bounds__(256) k_batch_march(const BProb* __restrict__ p
 
 // Full weighting (restriction) or trilinear prolongation between the levels of
 // every listed problem.  Tiles cover the destination level.
-template <typename T, class F>
-__device__ __forceinline__ T fw(const F& f, bool bI, bool bJ, bool bK)
-{
-    if (bI && bJ && bK) return f(0, 0, 0);
-    if (bJ && bK) return (T)0.25 * f(-1, 0, 0) + (T)0.5 * f(0, 0, 0) + (T)0.25 * f(1, 0, 0);
-    if (bK && bI) return (T)0.25 * f(0, -1, 0) + (T)0.5 * f(0, 0, 0) + (T)0.25 * f(0, 1, 0);
-    if (bI && bJ) return (T)0.25 * f(0, 0, -1) + (T)0.5 * f(0, 0, 0) + (T)0.25 * f(0, 0, 1);
-    if (bI)
-        return (f(0, -1, -1) + (T)2 * f(0, 0, -1) + f(0, 1, -1) + (T)2 * f(0, -1, 0) + (T)4 * f(0, 0, 0) +
-                (T)2 * f(0, 1, 0) + f(0, -1, 1) + (T)2 * f(0, 0, 1) + f(0, 1, 1)) * (T)(1.0 / 16.0);
-    if (bJ)
-        return (f(-1, 0, -1) + (T)2 * f(-1, 0, 0) + f(-1, 0, 1) + (T)2 * f(0, 0, -1) + (T)4 * f(0, 0, 0) +
-                (T)2 * f(0, 0, 1) + f(1, 0, -1) + (T)2 * f(1, 0, 0) + f(1, 0, 1)) * (T)(1.0 / 16.0);
-    if (bK)
-        return (f(-1, -1, 0) + (T)2 * f(0, -1, 0) + f(1, -1, 0) + (T)2 * f(-1, 0, 0) + (T)4 * f(0, 0, 0) +
-                (T)2 * f(1, 0, 0) + f(-1, 1, 0) + (T)2 * f(0, 1, 0) + f(1, 1, 0)) * (T)(1.0 / 16.0);
-    return (f(-1, -1, -1) + f(-1, -1, 1) + f(-1, 1, -1) + f(-1, 1, 1) + f(1, -1, -1) + f(1, -1, 1) + f(1, 1, -1) +
-            f(1, 1, 1)) * (T)(1.0 / 64.0) +
-           (f(0, -1, -1) + f(0, -1, 1) + f(0, 1, -1) + f(0, 1, 1) + f(-1, 0, -1) + f(1, 0, -1) + f(-1, 0, 1) +
-            f(1, 0, 1) + f(-1, -1, 0) + f(-1, 1, 0) + f(1, -1, 0) + f(1, 1, 0)) * (T)(1.0 / 32.0) +
-           (f(-1, 0, 0) + f(0, -1, 0) + f(0, 0, -1) + f(1, 0, 0) + f(0, 1, 0) + f(0, 0, 1)) * (T)(1.0 / 16.0) +
-           f(0, 0, 0) * (T)(1.0 / 8.0);
-}
-
-__device__ __forceinline__ int bwrap(int i, int n, int per)
-{
-    if (per) {
-        if (i < 0) return i + n;
-        if (i >= n) return i - n;
-    }
-    return i;
-}
-
 template <typename T>
 __global__ void __launch_bounds__(256) k_batch_transfer(int restrict_not_interp, int assign,
                                                         const BProb* __restrict__ pf, const BProb* __restrict__ pc,
@@ -442,31 +386,21 @@ __global__ void __launch_bounds__(256) k_batch_transfer(int restrict_not_interp,
             for (int c = 0; c < 3; c++) {
                 const T* s = src + pf[tl.prob].vo + c * Lf.S;
                 auto f = [&](int a, int b, int d) -> T {
-                    return __ldg(s + Lf.idx(bwrap(2 * i + a, Lf.n[0], Lf.per[0]), bwrap(2 * j + b, Lf.n[1], Lf.per[1]),
-                                            bwrap(2 * k + d, Lf.n[2], Lf.per[2])));
+                    return __ldg(s + Lf.idx(wrapn(2 * i + a, Lf.n[0], Lf.per[0]), wrapn(2 * j + b, Lf.n[1], Lf.per[1]),
+                                            wrapn(2 * k + d, Lf.n[2], Lf.per[2])));
                 };
-                dst[q + c * Lc.S] = fw<T>(f, bI, bJ, bK);
+                dst[q + c * Lc.S] = full_weight<T>(f, bI, bJ, bK);
             }
         } else {
             const int I = i >> 1, J = j >> 1, K = k >> 1;
-            const int I1 = bwrap(I + 1, Lc.n[0], Lc.per[0]), J1 = bwrap(J + 1, Lc.n[1], Lc.per[1]),
-                      K1 = bwrap(K + 1, Lc.n[2], Lc.per[2]);
+            const int I1 = wrapn(I + 1, Lc.n[0], Lc.per[0]), J1 = wrapn(J + 1, Lc.n[1], Lc.per[1]),
+                      K1 = wrapn(K + 1, Lc.n[2], Lc.per[2]);
             const bool ei = !(i & 1), ej = !(j & 1), ek = !(k & 1);
             const long long q = pf[tl.prob].vo + Lf.idx(i, j, k);
             for (int c = 0; c < 3; c++) {
                 const T* cs = src + pc[tl.prob].vo + c * Lc.S;
                 auto C = [&](int a, int b, int d) -> T { return __ldg(cs + Lc.idx(a ? I1 : I, b ? J1 : J, d ? K1 : K)); };
-                T v;
-                if (ei && ej && ek) v = C(0, 0, 0);
-                else if (ej && ek) v = (T)0.5 * (C(0, 0, 0) + C(1, 0, 0));
-                else if (ek && ei) v = (T)0.5 * (C(0, 0, 0) + C(0, 1, 0));
-                else if (ei && ej) v = (T)0.5 * (C(0, 0, 0) + C(0, 0, 1));
-                else if (ei) v = (T)0.25 * (C(0, 0, 0) + C(0, 1, 0) + C(0, 0, 1) + C(0, 1, 1));
-                else if (ej) v = (T)0.25 * (C(0, 0, 0) + C(0, 0, 1) + C(1, 0, 0) + C(1, 0, 1));
-                else if (ek) v = (T)0.25 * (C(0, 0, 0) + C(1, 0, 0) + C(0, 1, 0) + C(1, 1, 0));
-                else
-                    v = (T)0.125 * (C(0, 0, 0) + C(1, 0, 0) + C(0, 1, 0) + C(0, 0, 1) + C(0, 1, 1) + C(1, 0, 1) +
-                                    C(1, 1, 0) + C(1, 1, 1));
+                const T v = interp_node<T>(C, ei, ej, ek);
                 T* o = dst + q + c * Lf.S;
                 *o = assign ? v : (*o + v);
             }
@@ -492,10 +426,10 @@ __global__ void __launch_bounds__(256) k_batch_avg_ddw(const BProb* __restrict__
         for (int m = 0; m < ncoef; m++) {
             const double* s = fine + pf[tl.prob].co + m * Lf.S;
             auto f = [&](int a, int b, int d) -> double {
-                return s[Lf.idx(bwrap(2 * I + a, Lf.n[0], Lf.per[0]), bwrap(2 * J + b, Lf.n[1], Lf.per[1]),
-                                bwrap(2 * K + d, Lf.n[2], Lf.per[2]))];
+                return s[Lf.idx(wrapn(2 * I + a, Lf.n[0], Lf.per[0]), wrapn(2 * J + b, Lf.n[1], Lf.per[1]),
+                                wrapn(2 * K + d, Lf.n[2], Lf.per[2]))];
             };
-            crse[q + m * Lc.S] = fw<double>(f, bI, bJ, bK);
+            crse[q + m * Lc.S] = full_weight<double>(f, bI, bJ, bK);
         }
     }
 }
@@ -628,7 +562,7 @@ __device__ void bapply(const BProb& P, const BCTable& bc, int uniform, const R* 
     for (long long e = threadIdx.x; e < cnt; e += blockDim.x) {
         const int i = (int)(e % L.nn[0]), j = (int)((e / L.nn[0]) % L.nn[1]),
                   k = (int)(e / ((long long)L.nn[0] * L.nn[1]));
-        BAcc<R> acc{x, ddw, L.S, bnbr(L, i, j, k)};
+        BAcc<R> acc{x, ddw, L.S, make_nbr(L, i, j, k)};
         const int pos[3] = {i, j, k};
         int mn[3], mx[3];
         bool bnd = false;
@@ -812,7 +746,7 @@ __global__ void __launch_bounds__(256) k_batch_rhs(const BProb* __restrict__ pro
         const LevelDesc& L = P.L;
         int i, j, k;
         if (!tile_node<32, 4, 2>(tl, L, i, j, k)) continue;
-        const BNbr nb = bnbr(L, i, j, k);
+        const Nbr nb = make_nbr(L, i, j, k);
         double E[3][3];
         for (int a = 0; a < 3; a++)
             for (int c = 0; c < 3; c++) E[a][c] = 0.0 - F0[tl.prob * 9 + a * 3 + c];
@@ -848,7 +782,7 @@ __global__ void __launch_bounds__(256) k_batch_mean_stress(const BProb* __restri
         int i, j, k;
         double S[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
         if (tile_node<32, 4, 2>(tl, L, i, j, k)) {
-            const BNbr nb = bnbr(L, i, j, k);
+            const Nbr nb = make_nbr(L, i, j, k);
             double G[3][3], c[NCoef<SYM>::value];
             for (int p = 0; p < 3; p++)
                 for (int d = 0; d < 3; d++)

@@ -17,6 +17,8 @@
 #include <cuda_runtime.h>
 
 #include <cstdlib>
+#include <cstring>
+
 
 #include "agb_internal.h"
 #include "stencil.cuh"
@@ -344,38 +346,186 @@ __global__ void k_bottom_assemble(LevelDesc L, BCTable bc, Geo<double> g, int un
     for (int c = 0; c < 3; c++) A[(long long)col * nu + c * cnt + e] = f[c];
 }
 
-// The BiCGStab + smoothing of k_bottom on the dense operator, one thread per
-// unknown (DENSE_MAX threads), arithmetic in R.  The FP64 solve runs it in
-// FP64; the FP32 cycles of the mixed solve run it in FP32, like the rest of
-// their cycle (GB300's FP64 rate per SM sub-partition is about 1/64 of its
-// FP32 rate, so an FP64 bottom solve would cost more than the FP32 cycle
-// around it).
-template <typename R> struct DenseRed {
-    R* red;   // shared, 3 * (DENSE_MAX / 32)
-    __device__ __forceinline__ R sum(R v) const
+// The BiCGStab + smoothing of k_bottom on the dense operator, arithmetic in R.
+// The FP64 solve runs it in FP64; the FP32 cycles of the mixed solve run it in
+// FP32, like the rest of their cycle (GB300's FP64 rate per SM sub-partition
+// is about 1/64 of its FP32 rate, so an FP64 bottom solve would cost more than
+// the FP32 cycle around it).  The operator sits in shared memory
+// (column-major, A[j * nu + q] = (A e_j)_q); thread q < nu owns unknown q and
+// every thread of the CTA takes part in the barriers.  Each reduction costs
+// one barrier: warps reduce by shuffles, write their partials to one of two
+// alternating buffers, and after the barrier every thread combines the
+// partials in warp order (so all threads hold the same value and take the
+// same branches).  Reductions that need no value in between share a barrier:
+// (max|r|, rh.r) at the end of an iteration, (t.t, t.s), and the publication
+// of s with max|s|.  A x sums over j in ascending order, as k_bottom's rows do.
+enum { RED_SUM = 0, RED_MAX = 1 };
+
+template <typename R> struct BlockRed {
+    R* red;    // shared: 2 buffers x 3 values x 32 warps
+    int buf;
+    template <int N>
+    __device__ __forceinline__ void run(R (&v)[N], const int (&op)[N])
     {
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        __syncthreads();
-        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-        __syncthreads();
-        R t = 0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w];
-        return t;
-    }
-    __device__ __forceinline__ R max(R v) const
-    {
-        for (int o = 16; o > 0; o >>= 1) {
-            const R w = __shfl_xor_sync(0xffffffffu, v, o);
-            v = (w > v || w != w) ? w : v;
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (int)(blockDim.x >> 5);
+#pragma unroll
+        for (int k = 0; k < N; k++) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const R w = __shfl_xor_sync(0xffffffffu, v[k], o);
+                if (op[k] == RED_SUM) v[k] += w;
+                else v[k] = (w > v[k] || w != w) ? w : v[k];
+            }
+            if (lane == 0) red[(buf * 3 + k) * 32 + warp] = v[k];
         }
         __syncthreads();
-        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-        __syncthreads();
-        R t = 0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t = (red[w] > t || red[w] != red[w]) ? red[w] : t;
-        return t;
+#pragma unroll
+        for (int k = 0; k < N; k++) {
+            R t = red[(buf * 3 + k) * 32];
+            for (int w = 1; w < nw; w++) {
+                const R x = red[(buf * 3 + k) * 32 + w];
+                if (op[k] == RED_SUM) t += x;
+                else t = (x > t || x != x) ? x : t;
+            }
+            v[k] = t;
+        }
+        buf ^= 1;
     }
 };
+
+// Right-hand side read with L2-coherent loads (it may have been written
+// earlier in the same kernel by other CTAs).  `red` holds 2 x 3 x 32 values.
+template <typename T, typename R>
+__device__ void dense_bottom_block(const LevelDesc& L, const R* __restrict__ A, R* __restrict__ xs, R* __restrict__ red,
+                                   const double* __restrict__ diag, T* __restrict__ cor, const T* __restrict__ res,
+                                   int maxiter, double eps_rel_d, double eps_abs_d, int nub, int nuf, double omega_d,
+                                   int* ret_slot)
+{
+    const int cnt = (int)L.count(), nu = 3 * cnt;
+    const int q = threadIdx.x;
+    const bool ok = q < nu;
+    const int comp = ok ? q / cnt : 0;
+    const long long pq = ok ? dense_to_padded(L, q, cnt) : 0;
+    const R b = ok ? (R)__ldcg(res + pq) : (R)0;
+    const R d = ok ? (R)diag[pq] : (R)1;
+    const R eps_rel = (R)eps_rel_d, eps_abs = (R)eps_abs_d, omega = (R)omega_d;
+    const bool sing = L.singular();
+    BlockRed<R> br{red, 0};
+    // y = A x for the vector published in xs
+    auto product = [&]() -> R {
+        R y = 0;
+        if (ok)
+            for (int j = 0; j < nu; j++) y += A[j * nu + q] * xs[j];
+        return y;
+    };
+    auto publish = [&](R x) {
+        if (ok) xs[q] = x;
+    };
+    // zero-mean projection per component (fully periodic level)
+    auto project = [&](R v) -> R {
+        R m[3] = {ok && comp == 0 ? v : (R)0, ok && comp == 1 ? v : (R)0, ok && comp == 2 ? v : (R)0};
+        const int op[3] = {RED_SUM, RED_SUM, RED_SUM};
+        br.run(m, op);
+        const R mc = comp == 0 ? m[0] : (comp == 1 ? m[1] : m[2]);
+        return ok ? v - mc / (R)cnt : (R)0;
+    };
+    R sol = 0, r = 0, rh = 0, p = 0, v = 0, sv = 0, t = 0;
+    // r = P(b - A*0)/D, P the zero-mean projection on a singular level
+    const R bp = sing ? project(b) : b;
+    if (ok) {
+        r = bp / d;
+        rh = r;
+    }
+    R rnorm, rho;
+    {
+        R m[2] = {fabs(r), rh * r};
+        const int op[2] = {RED_MAX, RED_SUM};
+        br.run(m, op);
+        rnorm = m[0];
+        rho = m[1];
+    }
+    const R rnorm0 = rnorm;
+    int ret = 0;
+    R rho_1 = 0, alpha = 0, om = 0;
+    if (!(rnorm0 == 0 || rnorm0 < eps_abs)) {
+        for (int iter = 1; iter <= maxiter; iter++) {
+            if (rho == 0) { ret = 1; break; }
+            if (iter == 1) p = r;
+            else {
+                const R beta = (rho / rho_1) * (alpha / om);
+                p = r + beta * (p - om * v);
+            }
+            // every thread finished reading xs (last product) before the last barrier
+            publish(p);
+            __syncthreads();
+            v = product();
+            if (sing) v = project(v);
+            v = ok ? v / d : (R)0;
+            {
+                R m[1] = {rh * v};
+                const int op[1] = {RED_SUM};
+                br.run(m, op);
+                if (m[0] != 0) alpha = rho / m[0];
+                else { ret = 2; break; }
+            }
+            sol += alpha * p;
+            sv = r - alpha * v;
+            publish(sv);   // xs is free: every product(p) finished before the rh.v barrier
+            {
+                R m[1] = {fabs(sv)};
+                const int op[1] = {RED_MAX};
+                br.run(m, op);
+                rnorm = m[0];
+            }
+            if (rnorm < eps_rel * rnorm0 || rnorm < eps_abs) break;
+            t = product();
+            if (sing) t = project(t);
+            t = ok ? t / d : (R)0;
+            {
+                R m[2] = {t * t, t * sv};
+                const int op[2] = {RED_SUM, RED_SUM};
+                br.run(m, op);
+                if (m[0] != 0) om = m[1] / m[0];
+                else { ret = 3; break; }
+            }
+            sol += om * sv;
+            r = sv - om * t;
+            rho_1 = rho;
+            {
+                R m[2] = {fabs(r), rh * r};
+                const int op[2] = {RED_MAX, RED_SUM};
+                br.run(m, op);
+                rnorm = m[0];
+                rho = m[1];
+            }
+            if (rnorm < eps_rel * rnorm0 || rnorm < eps_abs) break;
+            if (om == 0) { ret = 4; break; }
+        }
+        if (ret == 0 && rnorm > eps_rel * rnorm0 && rnorm > eps_abs) ret = 8;
+        // MLMG::actualBottomSolve: anything but a clean solve discards the correction
+        if (ret != 0 || !(rnorm < rnorm0)) sol = 0;
+    }
+    // post-smoothing: Fsmooth = 2 Jacobi sweeps each
+    const int nsm = 2 * ((ret == 0) ? nub : nuf);
+    for (int sw = 0; sw < nsm; sw++) {
+        __syncthreads();   // the last product finished with xs
+        publish(sol);
+        __syncthreads();
+        const R Ax = product();
+        if (ok) {
+            const R Rx = Ax - sol * d;
+            sol = ((R)1 - omega) * sol + omega * (b - Rx) / d;
+        }
+    }
+    if (ok) cor[pq] = (T)sol;
+    if (threadIdx.x == 0 && ret_slot) *ret_slot = ret;
+}
+
+// The CTA copies the operator (FP64, column-major) into shared memory in R.
+template <typename R> __device__ __forceinline__ void dense_load(R* A, const double* __restrict__ Ag, int nu)
+{
+    for (int q = threadIdx.x; q < nu * nu; q += blockDim.x) A[q] = (R)Ag[q];
+}
 
 template <typename T, typename R>
 __global__ void __launch_bounds__(DENSE_MAX) k_bottom_dense(LevelDesc L, const double* __restrict__ Ag,
@@ -385,98 +535,13 @@ __global__ void __launch_bounds__(DENSE_MAX) k_bottom_dense(LevelDesc L, const d
                                                             int* ret_slot)
 {
     extern __shared__ __align__(16) unsigned char dsm_raw[];
-    const int cnt = (int)L.count(), nu = 3 * cnt;
+    __shared__ R red[2 * 3 * 32];
+    const int nu = 3 * (int)L.count();
     R* A = reinterpret_cast<R*>(dsm_raw);
-    R* xs = A + nu * nu;
-    __shared__ R red_s[DENSE_MAX / 32];
-    const DenseRed<R> red{red_s};
-    for (int q = threadIdx.x; q < nu * nu; q += blockDim.x) A[q] = (R)Ag[q];
-    const int q = threadIdx.x;
-    const bool ok = q < nu;
-    const int comp = ok ? q / cnt : 0;
-    const long long pq = ok ? dense_to_padded(L, q, cnt) : 0;
-    const R b = ok ? (R)res[pq] : (R)0;
-    const R d = ok ? (R)diag[pq] : (R)1;
-    const R eps_rel = (R)eps_rel_d, eps_abs = (R)eps_abs_d, omega = (R)omega_d;
-    const bool sing = L.singular();
+    dense_load<R>(A, Ag, nu);
     __syncthreads();
-    // y = A x (x staged through shared memory)
-    auto matvec = [&](R x) -> R {
-        __syncthreads();
-        if (ok) xs[q] = x;
-        __syncthreads();
-        R y = 0;
-        if (ok)
-            for (int j = 0; j < nu; j++) y += A[j * nu + q] * xs[j];
-        return y;
-    };
-    // zero-mean projection per component (fully periodic level)
-    auto project = [&](R v) -> R {
-        const R s0 = red.sum(ok && comp == 0 ? v : (R)0);
-        const R s1 = red.sum(ok && comp == 1 ? v : (R)0);
-        const R s2 = red.sum(ok && comp == 2 ? v : (R)0);
-        const R m = comp == 0 ? s0 : (comp == 1 ? s1 : s2);
-        return ok ? v - m / (R)cnt : (R)0;
-    };
-    R sol = 0, r = 0, rh = 0, p = 0, v = 0, s = 0, t = 0;
-    // r = P(b - A*0)/D, P the zero-mean projection on a singular level
-    const R bp = sing ? project(b) : b;
-    if (ok) {
-        r = bp / d;
-        rh = r;
-    }
-    R rnorm = red.max(fabs(r));
-    const R rnorm0 = rnorm;
-    int ret = 0;
-    R rho_1 = 0, alpha = 0, om = 0;
-    if (!(rnorm0 == 0 || rnorm0 < eps_abs)) {
-        for (int iter = 1; iter <= maxiter; iter++) {
-            const R rho = red.sum(rh * r);
-            if (rho == 0) { ret = 1; break; }
-            if (iter == 1) p = r;
-            else {
-                const R beta = (rho / rho_1) * (alpha / om);
-                p = r + beta * (p - om * v);
-            }
-            v = matvec(p);
-            if (sing) v = project(v);
-            v = ok ? v / d : (R)0;
-            const R rhTv = red.sum(rh * v);
-            if (rhTv != 0) alpha = rho / rhTv;
-            else { ret = 2; break; }
-            sol += alpha * p;
-            s = r - alpha * v;
-            rnorm = red.max(fabs(s));
-            if (rnorm < eps_rel * rnorm0 || rnorm < eps_abs) break;
-            t = matvec(s);
-            if (sing) t = project(t);
-            t = ok ? t / d : (R)0;
-            const R tt = red.sum(t * t);
-            const R ts = red.sum(t * s);
-            if (tt != 0) om = ts / tt;
-            else { ret = 3; break; }
-            sol += om * s;
-            r = s - om * t;
-            rnorm = red.max(fabs(r));
-            if (rnorm < eps_rel * rnorm0 || rnorm < eps_abs) break;
-            if (om == 0) { ret = 4; break; }
-            rho_1 = rho;
-        }
-        if (ret == 0 && rnorm > eps_rel * rnorm0 && rnorm > eps_abs) ret = 8;
-        // MLMG::actualBottomSolve: anything but a clean solve discards the correction
-        if (ret != 0 || !(rnorm < rnorm0)) sol = 0;
-    }
-    // post-smoothing: Fsmooth = 2 Jacobi sweeps each
-    const int nsm = 2 * ((ret == 0) ? nub : nuf);
-    for (int sw = 0; sw < nsm; sw++) {
-        const R Ax = matvec(sol);
-        if (ok) {
-            const R Rx = Ax - sol * d;
-            sol = ((R)1 - omega) * sol + omega * (b - Rx) / d;
-        }
-    }
-    if (ok) cor[pq] = (T)sol;
-    if (threadIdx.x == 0 && ret_slot) *ret_slot = ret;
+    dense_bottom_block<T, R>(L, A, A + nu * nu, red, diag, cor, res, maxiter, eps_rel_d, eps_abs_d, nub, nuf, omega_d,
+                             ret_slot);
 }
 
 bool bottom_dense_fits(const LevelDesc& L) { return 3 * L.count() <= DENSE_MAX; }

@@ -70,31 +70,6 @@ __device__ __forceinline__ void block_max_to_slot(T v, void* slot)
     }
 }
 
-// Neighbour offsets of a node, periodic images folded in.
-struct Nbr {
-    long long base;
-    long long o[3][3];   // o[d][delta+1]
-};
-
-__device__ __forceinline__ Nbr make_nbr(const LevelDesc& L, int i, int j, int k)
-{
-    Nbr nb;
-    nb.base = L.idx(i, j, k);
-    const long long st[3] = {1, (long long)L.P, (long long)L.P * L.nn[1]};
-    const int pos[3] = {i, j, k};
-#pragma unroll
-    for (int d = 0; d < 3; d++) {
-        nb.o[d][0] = -st[d];
-        nb.o[d][1] = 0;
-        nb.o[d][2] = st[d];
-        if (L.per[d]) {
-            if (pos[d] == 0) nb.o[d][0] = st[d] * (L.n[d] - 1);
-            if (pos[d] == L.n[d] - 1) nb.o[d][2] = -st[d] * (L.n[d] - 1);
-        }
-    }
-    return nb;
-}
-
 template <typename T> struct GlobalAcc {
     const T* __restrict__ x;
     const T* __restrict__ c;

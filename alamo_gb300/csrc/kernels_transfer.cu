@@ -9,48 +9,13 @@
 #include <cuda_runtime.h>
 
 #include "agb_internal.h"
+#include "transfer.cuh"
 
 namespace agb {
-
-__device__ __forceinline__ int wrapn(int i, int n, int per)
-{
-    if (per) {
-        if (i < 0) return i + n;
-        if (i >= n) return i - n;
-    }
-    return i;
-}
 
 static inline dim3 grid_for(const LevelDesc& L, dim3 blk)
 {
     return dim3((L.nn[0] + blk.x - 1) / blk.x, (L.nn[1] + blk.y - 1) / blk.y, (L.nn[2] + blk.z - 1) / blk.z);
-}
-
-// Nodal full weighting with lower-dimensional stencils on the coarse domain
-// boundary; the same weights serve the residual restriction and the modulus
-// averaging.  F(a,b,c) returns the fine value at (2I+a, 2J+b, 2K+c).
-template <typename T, class F>
-__device__ __forceinline__ T full_weight(const F& f, bool bI, bool bJ, bool bK)
-{
-    if (bI && bJ && bK) return f(0, 0, 0);
-    if (bJ && bK) return (T)0.25 * f(-1, 0, 0) + (T)0.5 * f(0, 0, 0) + (T)0.25 * f(1, 0, 0);
-    if (bK && bI) return (T)0.25 * f(0, -1, 0) + (T)0.5 * f(0, 0, 0) + (T)0.25 * f(0, 1, 0);
-    if (bI && bJ) return (T)0.25 * f(0, 0, -1) + (T)0.5 * f(0, 0, 0) + (T)0.25 * f(0, 0, 1);
-    if (bI)
-        return (f(0, -1, -1) + (T)2 * f(0, 0, -1) + f(0, 1, -1) + (T)2 * f(0, -1, 0) + (T)4 * f(0, 0, 0) +
-                (T)2 * f(0, 1, 0) + f(0, -1, 1) + (T)2 * f(0, 0, 1) + f(0, 1, 1)) * (T)(1.0 / 16.0);
-    if (bJ)
-        return (f(-1, 0, -1) + (T)2 * f(-1, 0, 0) + f(-1, 0, 1) + (T)2 * f(0, 0, -1) + (T)4 * f(0, 0, 0) +
-                (T)2 * f(0, 0, 1) + f(1, 0, -1) + (T)2 * f(1, 0, 0) + f(1, 0, 1)) * (T)(1.0 / 16.0);
-    if (bK)
-        return (f(-1, -1, 0) + (T)2 * f(0, -1, 0) + f(1, -1, 0) + (T)2 * f(-1, 0, 0) + (T)4 * f(0, 0, 0) +
-                (T)2 * f(1, 0, 0) + f(-1, 1, 0) + (T)2 * f(0, 1, 0) + f(1, 1, 0)) * (T)(1.0 / 16.0);
-    return (f(-1, -1, -1) + f(-1, -1, 1) + f(-1, 1, -1) + f(-1, 1, 1) + f(1, -1, -1) + f(1, -1, 1) + f(1, 1, -1) +
-            f(1, 1, 1)) * (T)(1.0 / 64.0) +
-           (f(0, -1, -1) + f(0, -1, 1) + f(0, 1, -1) + f(0, 1, 1) + f(-1, 0, -1) + f(1, 0, -1) + f(-1, 0, 1) +
-            f(1, 0, 1) + f(-1, -1, 0) + f(-1, 1, 0) + f(1, -1, 0) + f(1, 1, 0)) * (T)(1.0 / 32.0) +
-           (f(-1, 0, 0) + f(0, -1, 0) + f(0, 0, -1) + f(1, 0, 0) + f(0, 1, 0) + f(0, 0, 1)) * (T)(1.0 / 16.0) +
-           f(0, 0, 0) * (T)(1.0 / 8.0);
 }
 
 // Fine-level offsets of the nodes 2I-1, 2I, 2I+1 (periodic wrap) in the three

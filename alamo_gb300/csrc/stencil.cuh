@@ -168,6 +168,31 @@ __device__ __forceinline__ void dC_col(const A& acc, const T G[3][3], T out[3])
     }
 }
 
+// Neighbour offsets of a node, periodic images folded in.
+struct Nbr {
+    long long base;
+    long long o[3][3];   // o[d][delta+1]
+};
+
+__device__ __forceinline__ Nbr make_nbr(const LevelDesc& L, int i, int j, int k)
+{
+    Nbr nb;
+    nb.base = L.idx(i, j, k);
+    const long long st[3] = {1, (long long)L.P, (long long)L.P * L.nn[1]};
+    const int pos[3] = {i, j, k};
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        nb.o[d][0] = -st[d];
+        nb.o[d][1] = 0;
+        nb.o[d][2] = st[d];
+        if (L.per[d]) {
+            if (pos[d] == 0) nb.o[d][0] = st[d] * (L.n[d] - 1);
+            if (pos[d] == L.n[d] - 1) nb.o[d][2] = -st[d] * (L.n[d] - 1);
+        }
+    }
+    return nb;
+}
+
 // ---------------------------------------------------------------------------
 // Interior row.  A provides u(c,di,dj,dk) and C(m,di,dj,dk) relative to the node.
 // ---------------------------------------------------------------------------
