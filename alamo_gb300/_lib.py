@@ -43,6 +43,7 @@ class AgbSolverParams(ctypes.Structure):
         ("inner_max_iter", ctypes.c_int),
         ("max_refine", ctypes.c_int),
         ("use_graph", ctypes.c_int),
+        ("krylov", ctypes.c_int),
     ]
 
 

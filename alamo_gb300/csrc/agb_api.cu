@@ -127,6 +127,13 @@ struct agb_solver_s {
     int g64_fcycle = -1, g32_fcycle = -1;   // cycle kind each graph holds
     long long g64_kernels = 0, g32_kernels = 0;
     long long replayed = 0;                  // kernels executed through graph replays
+    // inner FP32 GCR of the mixed solve (params.krylov > 0): directions, their
+    // images, the inner residual, device scalars, the preconditioner's graph
+    std::vector<float*> kZ, kW;
+    float* kr = nullptr;
+    double* kdots = nullptr;
+    cudaGraphExec_t gpre = nullptr;
+    long long gpre_kernels = 0;
     // flexible GCR (agb_learned_solve): stored directions and work vectors
     std::vector<double*> gZ, gW;
     double *gr = nullptr, *gz = nullptr, *gw = nullptr, *grv = nullptr, *ge = nullptr, *gt = nullptr;
@@ -631,6 +638,112 @@ agb_status solve_plain(agb_solver s, double tol_rel, double tol_abs, agb_solve_r
     return st;
 }
 
+// The preconditioner of the inner GCR: one FP32 cycle (F-cycle unless
+// max_fmg_iter is 0) on the inner residual, leaving its result in cor32(0).
+void precond32_body(agb_solver s)
+{
+    agb_op op = s->op;
+    Engine<float> E{op, s->p};
+    Level& v0 = op->lev[0];
+    cudaMemcpyAsync(v0.res32, s->kr, sizeof(float) * 3 * (size_t)v0.L.S, cudaMemcpyDeviceToDevice, op->st);
+    E.cycle(0);
+}
+
+agb_status run_precond32(agb_solver s)
+{
+    agb_op op = s->op;
+    if (!s->p.use_graph) {
+        precond32_body(s);
+        CK(cudaGetLastError());
+        return AGB_OK;
+    }
+    if (!s->gpre) {
+        const long long k0 = launch_counter();
+        TRY(capture(op, &s->gpre, [&] { precond32_body(s); }));
+        s->gpre_kernels = launch_counter() - k0;
+        launch_counter() = k0;
+    }
+    CK(cudaGraphLaunch(s->gpre, op->st));
+    s->replayed += s->gpre_kernels;
+    return AGB_OK;
+}
+
+// Inner solve A c = f (f = rhs32, c = sol32 zeroed by the caller) by flexible
+// GCR with up to params.krylov stored directions (restarted when full): each
+// iteration adds the direction z = M r, M one FP32 cycle, with w = A z
+// orthogonalised against the stored w's (classical Gram-Schmidt) in the
+// inner product <a, b> = sum a b / diag^2, and minimises the residual over
+// it.  Every iteration lowers the weighted residual norm, whatever the
+// orthogonality of the stored directions; the weights put displacement,
+// traction and interior rows on one scale.  On a fully periodic box w is
+// projected to zero mean like every residual.  Stops when max |r| <=
+// inner_tol (f has max norm 1), when it stalls, or after inner_max_iter
+// iterations (each one cycle).
+agb_status inner_gcr32(agb_solver s, double inner_tol, double* inorm_out, int* cycles)
+{
+    agb_op op = s->op;
+    Level& v0 = op->lev[0];
+    const LevelDesc& L = v0.L;
+    const int m = std::max(1, std::min(s->p.krylov, GCR_MAX));
+    const long long n = 3 * L.S;
+    const size_t bytes = sizeof(float) * (size_t)n;
+    while ((int)s->kZ.size() < m) {
+        float *z = nullptr, *w = nullptr;
+        TRY(op->alloc(&z, (size_t)n));
+        TRY(op->alloc(&w, (size_t)n));
+        s->kZ.push_back(z);
+        s->kW.push_back(w);
+    }
+    if (!s->kr) {
+        TRY(op->alloc(&s->kr, (size_t)n));
+        TRY(op->alloc(&s->kdots, GCR_MAX + 2));
+    }
+    cudaStream_t st = op->st;
+    const bool sing = L.singular();
+    CK(cudaMemcpyAsync(s->kr, s->rhs32, bytes, cudaMemcpyDeviceToDevice, st));
+    double inorm = 1.0, prev = 1.0;
+    int k = 0, slow = 0;
+    for (int it = 0; it < s->p.inner_max_iter; it++) {
+        if (k == m) k = 0;   // restart
+        TRY(run_precond32(s));
+        float* z = s->kZ[k];
+        float* w = s->kW[k];
+        CK(cudaMemcpyAsync(z, v0.cor32, bytes, cudaMemcpyDeviceToDevice, st));
+        launch_stencil<float>(st, op->sym, MODE_APPLY, L, op->bc, op->uniform, v0.ddw32, z, nullptr, nullptr, w, 0.0f,
+                              nullptr);
+        if (sing) launch_remove_mean<float>(st, L, w, op->d_slots + 11);
+        CK(cudaMemsetAsync(s->kdots, 0, sizeof(double) * (GCR_MAX + 2), st));
+        if (k > 0) {
+            GcrVecs W, Z;
+            for (int i = 0; i < k; i++) {
+                W.v[i] = s->kW[i];
+                Z.v[i] = s->kZ[i];
+            }
+            launch_multidot_w(st, n, k, w, W, v0.dinv32, s->kdots);
+            launch_gcr_orth(st, n, k, s->kdots, W, Z, w, z);
+        }
+        GcrVecs P;
+        P.v[0] = w;
+        P.v[1] = s->kr;
+        launch_multidot_w(st, n, 2, w, P, v0.dinv32, s->kdots + GCR_MAX);
+        CK(cudaMemsetAsync(op->d_slots + 1, 0, sizeof(double), st));
+        launch_gcr_step(st, n, s->kdots + GCR_MAX, w, z, s->sol32, s->kr, op->d_slots + 1);
+        CK(cudaMemcpyAsync(op->h_slots + 1, op->d_slots + 1, sizeof(double), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        inorm = slot_as_float(op->h_slots, 1);
+        k++;
+        (*cycles)++;
+        if (s->p.verbose) fprintf(stderr, "agb mixed GCR inner %d resid32 %.3e\n", it + 1, inorm);
+        if (std::isnan(inorm)) break;
+        if (inorm <= inner_tol) break;
+        slow = (inorm > 0.9 * prev) ? slow + 1 : 0;
+        if (slow >= 3) break;   // FP32 floor reached
+        prev = inorm;
+    }
+    *inorm_out = inorm;
+    return AGB_OK;
+}
+
 // FP32 cycles inside FP64 iterative refinement.
 agb_status solve_mixed(agb_solver s, double tol_rel, double tol_abs, agb_solve_report* rep)
 {
@@ -661,7 +774,8 @@ agb_status solve_mixed(agb_solver s, double tol_rel, double tol_abs, agb_solve_r
         const double inner_tol = std::max(s->p.inner_tol_rel, 0.3 * target / norm);
         double inorm = 1.0, prev = 1.0;
         int slow = 0;
-        for (int it = 0; it < s->p.inner_max_iter; it++) {
+        if (s->p.krylov > 0) TRY(inner_gcr32(s, inner_tol, &inorm, &total_cycles));
+        for (int it = 0; s->p.krylov <= 0 && it < s->p.inner_max_iter; it++) {
             TRY(run_iter32(s, it));
             CK(cudaStreamSynchronize(op->st));
             inorm = slot_as_float(op->h_slots, 1);
@@ -721,6 +835,7 @@ void agb_default_params(agb_solver_params* p)
     p->inner_max_iter = 60;
     p->max_refine = 20;
     p->use_graph = 1;
+    p->krylov = 0;
 }
 
 agb_status agb_op_create(const int n_cells[3], const double dx[3], const int periodic[3], int sym,
@@ -1026,6 +1141,10 @@ agb_status agb_solver_create(agb_op op, const agb_solver_params* params, agb_sol
         delete s;
         return fail(AGB_BADARG, "bad precision");
     }
+    if (s->p.krylov < 0 || s->p.krylov > GCR_MAX) {
+        delete s;
+        return fail(AGB_BADARG, "krylov must be in 0..%d", GCR_MAX);
+    }
     if (s->p.omega > 0) op->omega = s->p.omega;   // Linear::PrepareMLMG -> SetOmega
     const size_t n3 = 3 * (size_t)op->lev[0].L.S;
     agb_status st;
@@ -1048,6 +1167,7 @@ agb_status agb_solver_destroy(agb_solver s)
     if (!s) return AGB_OK;
     if (s->g64) cudaGraphExecDestroy(s->g64);
     if (s->g32) cudaGraphExecDestroy(s->g32);
+    if (s->gpre) cudaGraphExecDestroy(s->gpre);
     delete s;
     return AGB_OK;
 }

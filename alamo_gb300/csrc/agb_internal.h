@@ -172,6 +172,20 @@ template <typename TD, typename TS>
 void launch_export(cudaStream_t st, const LevelDesc& L, int ncomp, const TS* src, TD* dst, bool aos, int k0, int kc,
                    bool chunk);
 void launch_axpy_mixed(cudaStream_t st, const LevelDesc& L, int ncomp, double* y, const float* x, double a);
+// Inner FP32 GCR (kernels_transfer.cu): up to GCR_MAX stored directions.
+constexpr int GCR_MAX = 16;
+struct GcrVecs {
+    const float* v[GCR_MAX];
+};
+// out[i] += sum x v_i d^2 (i < k)
+void launch_multidot_w(cudaStream_t st, long long n, int k, const float* x, const GcrVecs& V, const float* d,
+                       double* out);
+// w -= sum beta_i W_i, z -= sum beta_i Z_i (i < k)
+void launch_gcr_orth(cudaStream_t st, long long n, int k, const double* beta, const GcrVecs& W, const GcrVecs& Z,
+                     float* w, float* z);
+// normalise (w, z) by sqrt(dots[0]), c += (dots[1] / dots[0]) z, r -= ... w, max |r| -> slot
+void launch_gcr_step(cudaStream_t st, long long n, const double* dots, float* w, float* z, float* c, float* r,
+                     void* slot);
 // *out += sum x[e] y[e] over n elements (padding entries are zero in every vector)
 void launch_dot(cudaStream_t st, long long n, const double* x, const double* y, double* out);
 // learned correction network (learned.cu)

@@ -381,6 +381,126 @@ void launch_dot(cudaStream_t st, long long n, const double* x, const double* y, 
     count_launch();
 }
 
+// ---------------------------------------------------------------------------
+// Vector kernels of the inner FP32 GCR (flexible, weighted inner product
+// <a, b> = sum a b d^2 with d = 1/diag: the rows of the operator scaled to a
+// unit diagonal, so that displacement, traction and interior rows weigh
+// alike).  All scalars stay on the device; sums accumulate in FP64.
+// ---------------------------------------------------------------------------
+
+// out[i] += sum_e x[e] v_i[e] d[e]^2, i < k (out zeroed by the caller).  Each
+// thread sums its elements in FP32 (a few dozen terms; FP64 arithmetic per
+// element would bind on GB300's FP64 rate); threads, warps and blocks are
+// combined in FP64.
+template <int K>
+__global__ void __launch_bounds__(256) k_multidot_w(long long n, const float* __restrict__ x, GcrVecs V,
+                                                    const float* __restrict__ d, double* __restrict__ out)
+{
+    float acc[K];
+#pragma unroll
+    for (int i = 0; i < K; i++) acc[i] = 0;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const float dd = d[e];
+        const float xw = x[e] * dd * dd;
+#pragma unroll
+        for (int i = 0; i < K; i++) acc[i] += xw * V.v[i][e];
+    }
+    __shared__ double red[8][K];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int k = K;
+#pragma unroll
+    for (int i = 0; i < K; i++) {
+        double a = (double)acc[i];
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+        if (lane == 0) red[warp][i] = a;
+    }
+    __syncthreads();
+    if (threadIdx.x < k) {
+        double t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w][threadIdx.x];
+        atomicAdd(out + threadIdx.x, t);
+    }
+}
+
+// w -= sum_i beta_i W_i and z -= sum_i beta_i Z_i, i < K (classical Gram-Schmidt step)
+template <int K>
+__global__ void k_gcr_orth(long long n, const double* __restrict__ beta, GcrVecs W, GcrVecs Z,
+                           float* __restrict__ w, float* __restrict__ z)
+{
+    float b[K];
+#pragma unroll
+    for (int i = 0; i < K; i++) b[i] = (float)beta[i];
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        float tw = w[e], tz = z[e];
+#pragma unroll
+        for (int i = 0; i < K; i++) {
+            tw -= b[i] * W.v[i][e];
+            tz -= b[i] * Z.v[i][e];
+        }
+        w[e] = tw;
+        z[e] = tz;
+    }
+}
+
+// With ww = <w, w> and rw = <r, w> (dots[0], dots[1]): w, z scaled to unit
+// norm, c += (rw / ww) z, r -= (rw / ww) w, and max |r| after it -> slot.
+__global__ void k_gcr_step(long long n, const double* __restrict__ dots, float* __restrict__ w,
+                           float* __restrict__ z, float* __restrict__ c, float* __restrict__ r, void* slot)
+{
+    const double ww = dots[0], rw = dots[1];
+    const float inv = ww > 0 ? (float)(1.0 / sqrt(ww)) : 0.0f;
+    const float a = ww > 0 ? (float)(rw / sqrt(ww)) : 0.0f;   // coefficient of the unit direction
+    float m = 0;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const float wu = w[e] * inv, zu = z[e] * inv;
+        w[e] = wu;
+        z[e] = zu;
+        c[e] += a * zu;
+        const float rn = r[e] - a * wu;
+        r[e] = rn;
+        const float t = fabsf(rn);
+        m = (t > m || t != t) ? t : m;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const float q = __shfl_xor_sync(0xffffffffu, m, o);
+        m = (q > m || q != q) ? q : m;
+    }
+    if ((threadIdx.x & 31) == 0) MaxSlot<float>::put(slot, m);
+}
+
+void launch_multidot_w(cudaStream_t st, long long n, int k, const float* x, const GcrVecs& V, const float* d,
+                       double* out)
+{
+    const int nb = blocks_1d(n);
+    switch (k) {
+#define K_(K) case K: k_multidot_w<K><<<nb, 256, 0, st>>>(n, x, V, d, out); break;
+        K_(1) K_(2) K_(3) K_(4) K_(5) K_(6) K_(7) K_(8) K_(9) K_(10) K_(11) K_(12) K_(13) K_(14) K_(15) K_(16)
+#undef K_
+    default: return;
+    }
+    count_launch();
+}
+
+void launch_gcr_orth(cudaStream_t st, long long n, int k, const double* beta, const GcrVecs& W, const GcrVecs& Z,
+                     float* w, float* z)
+{
+    const int nb = blocks_1d(n);
+    switch (k) {
+#define K_(K) case K: k_gcr_orth<K><<<nb, 256, 0, st>>>(n, beta, W, Z, w, z); break;
+        K_(1) K_(2) K_(3) K_(4) K_(5) K_(6) K_(7) K_(8) K_(9) K_(10) K_(11) K_(12) K_(13) K_(14) K_(15) K_(16)
+#undef K_
+    default: return;
+    }
+    count_launch();
+}
+
+void launch_gcr_step(cudaStream_t st, long long n, const double* dots, float* w, float* z, float* c, float* r,
+                     void* slot)
+{
+    k_gcr_step<<<blocks_1d(n), 256, 0, st>>>(n, dots, w, z, c, r, slot);
+    count_launch();
+}
+
 void launch_axpy_mixed(cudaStream_t st, const LevelDesc& L, int ncomp, double* y, const float* x, double a)
 {
     const long long n = (long long)ncomp * L.S;

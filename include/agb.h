@@ -96,6 +96,9 @@ typedef struct {
     int inner_max_iter;       /* mixed: FP32 cycles per refinement step (default 60) */
     int max_refine;           /* mixed: refinement steps (default 20) */
     int use_graph;            /* replay each cycle from a captured CUDA graph (default 1) */
+    int krylov;               /* mixed: 0 (default) = the FP32 cycles alone, as MLMG iterates; k in 1..16 =
+                                 flexible GCR over the FP32 cycle with up to k stored directions (an
+                                 extension: no reference counterpart) */
 } agb_solver_params;
 
 typedef struct {

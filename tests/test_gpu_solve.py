@@ -148,3 +148,36 @@ def test_status_codes(gpu_lib):
     with pytest.raises(AgbError) as e:
         op.Fapply(7, np.zeros(10))
     assert "AGB_BADARG" in str(e.value)
+
+
+@pytest.mark.parametrize("problem,n", [(c1_problem, 32), (c2_problem, 32), (c2_problem, 24)])
+def test_mixed_gcr_solve(gpu_lib, problem, n):
+    """FP32 cycles under flexible GCR (krylov = 8 stored directions) inside
+    FP64 refinement: reaches 1e-10 relative FP64 residual (checked by the
+    oracle's residual of the GPU solution) in fewer cycles than the FP32
+    cycles alone, and agrees with the FP64 oracle solve."""
+    from alamo_gb300 import Linear
+    g, ddw, F0, b, rhs = problem(n)
+    xo, rep_o = O.solve(g, ddw, rhs, tol_rel=1e-10, tol_abs=0.0)
+    op = gpu_op(g, ddw)
+    reps = {}
+    for kr in (0, 8):
+        sol = Linear(op, precision=1, krylov=kr)
+        x = np.zeros_like(rhs)
+        sol.solve(x, rhs, 1e-10, 0.0)
+        reps[kr] = sol.report
+        assert sol.report.status == 0
+        r = O.residual(g, ddw, x, rhs)
+        assert np.abs(r).max() <= 1e-10 * max(np.abs(rhs).max(), sol.report.res0) * 1.0000001
+        assert rel_err(x, xo) < 1e-6
+    print("cycles: FP32 cycles alone %d, under GCR %d" % (reps[0].iterations, reps[8].iterations))
+    assert reps[8].iterations < reps[0].iterations
+
+
+def test_mixed_gcr_rejects_bad_krylov(gpu_lib):
+    from alamo_gb300 import AgbError, Linear
+    g, ddw, F0, b, rhs = c1_problem(8)
+    op = gpu_op(g, ddw)
+    for kr in (-1, 17):
+        with pytest.raises(AgbError):
+            Linear(op, precision=1, krylov=kr)
