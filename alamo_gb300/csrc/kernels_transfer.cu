@@ -8,6 +8,8 @@
 //                     MultiFab components or AoS BaseFab<Matrix4>) <-> padded storage
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "agb_internal.h"
 #include "transfer.cuh"
 
@@ -201,6 +203,33 @@ __global__ void k_import(LevelDesc L, int ncomp, const TS* __restrict__ src, TD*
     for (int c = 0; c < ncomp; c++) dst[c * L.S + q] = (TD)(aos ? src[s * ncomp + c] : src[c * Nsrc + s]);
 }
 
+// The same for interleaved (AoS) sources, through shared memory: a warp
+// copies the contiguous 32 x ncomp source values of 32 consecutive nodes of a
+// row into shared memory (coalesced), then writes each component's 32 values
+// (coalesced).  Block (32, 8): one row segment per warp.
+template <typename TD, typename TS>
+__global__ void __launch_bounds__(256) k_import_aos(LevelDesc L, int ncomp, const TS* __restrict__ src,
+                                                   TD* __restrict__ dst, int k0, int kc, int chunk)
+{
+    extern __shared__ __align__(16) unsigned char imp_raw[];
+    TS* buf = reinterpret_cast<TS*>(imp_raw) + threadIdx.y * 32 * ncomp;
+    const int lane = threadIdx.x;
+    const long long r = (long long)blockIdx.y * blockDim.y + threadIdx.y;   // (j, k) row of the chunk
+    const int j = (int)(r % L.nn[1]);
+    const int k = k0 + (int)(r / L.nn[1]);
+    const int i0 = blockIdx.x * 32;
+    if (k >= k0 + kc || k >= L.nn[2]) return;   // uniform over the warp
+    const int cnt = min(32, L.nn[0] - i0);
+    const long long planeN = (long long)(L.n[0] + 1) * (L.n[1] + 1);
+    const long long sb = ((long long)i0 + (long long)(L.n[0] + 1) * j + planeN * (chunk ? k - k0 : k)) * ncomp;
+    for (int t = lane; t < cnt * ncomp; t += 32) buf[t] = src[sb + t];
+    __syncwarp();
+    if (lane < cnt) {
+        const long long q = L.idx(i0 + lane, j, k);
+        for (int c = 0; c < ncomp; c++) dst[c * L.S + q] = (TD)buf[lane * ncomp + c];
+    }
+}
+
 // padded storage -> reference nodal box for planes [k0, k0+kc) (periodic images filled)
 template <typename TD, typename TS>
 __global__ void k_export(LevelDesc L, int ncomp, const TS* __restrict__ src, TD* __restrict__ dst, int aos, int k0,
@@ -341,6 +370,15 @@ template <typename TD, typename TS>
 void launch_import(cudaStream_t st, const LevelDesc& L, int ncomp, const TS* src, TD* dst, bool aos, int k0, int kc,
                    bool chunk)
 {
+    if (aos && ncomp > 1 && ncomp <= 21) {
+        const dim3 blk(32, 8);
+        const long long rows = (long long)L.nn[1] * std::min(kc, L.nn[2] - k0);
+        const dim3 grd((L.nn[0] + 31) / 32, (unsigned)((rows + 7) / 8));
+        const size_t smem = 8 * 32 * (size_t)ncomp * sizeof(TS);
+        k_import_aos<TD, TS><<<grd, blk, smem, st>>>(L, ncomp, src, dst, k0, kc, chunk ? 1 : 0);
+        count_launch();
+        return;
+    }
     dim3 blk(32, 4, 2);
     dim3 grd((L.nn[0] + blk.x - 1) / blk.x, (L.nn[1] + blk.y - 1) / blk.y, (kc + blk.z - 1) / blk.z);
     k_import<TD, TS><<<grd, blk, 0, st>>>(L, ncomp, src, dst, aos ? 1 : 0, k0, kc, chunk ? 1 : 0); count_launch();
