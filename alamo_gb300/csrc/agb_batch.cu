@@ -461,9 +461,14 @@ agb_status residual0(agb_batch b, const int* act, const T* x, const T* rhs, T* r
     BLevel& v = b->lev[0];
     const bool sing = b->per[0] && b->per[1] && b->per[2];
     BCK(cudaMemsetAsync(b->d_norms, 0, sizeof(double) * b->np, b->st));
-    launch_batch_stencil<T>(b->st, b->sym, MODE_RESID, 0, b->grid, v.d_probs, compacted ? v.c_t32_full : v.d_t32_full,
-                            (int)v.t32_full.size(), act, b->bc, false, BArr<T>::ddw(v), x, rhs, nullptr, r, (T)0,
-                            sing ? nullptr : b->d_norms);
+    // the level's tuned tile list when it covers every problem (each has a
+    // coarser level), else the full list in the node-per-thread shape
+    bool tuned = b->tuned && !v.tS_smooth.empty();
+    for (int q = 0; tuned && q < b->np; q++) tuned = b->bottom[q] > 0;
+    const BTile* tl = tuned ? (compacted ? v.c_tS_smooth : v.d_tS_smooth) : (compacted ? v.c_t32_full : v.d_t32_full);
+    const int nt = tuned ? (int)v.tS_smooth.size() : (int)v.t32_full.size();
+    launch_batch_stencil<T>(b->st, b->sym, MODE_RESID, tuned ? v.shape : 0, b->grid, v.d_probs, tl, nt, act, b->bc,
+                            false, BArr<T>::ddw(v), x, rhs, nullptr, r, (T)0, sing ? nullptr : b->d_norms);
     if (sing) project<T>(b, act, r, true, compacted);
     BCK(cudaMemcpyAsync(b->h_norms, b->d_norms, sizeof(double) * b->np, cudaMemcpyDeviceToHost, b->st));
     return AGB_OK;

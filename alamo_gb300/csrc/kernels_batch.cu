@@ -820,8 +820,9 @@ __global__ void __launch_bounds__(256) k_batch_mean3(const BProb* __restrict__ p
     // its sums (or its max |y|) while the problem stays the same, and the CTA
     // reduces and flushes them with one atomic per value when it changes.
     __shared__ double red[3][8];
-    double s0 = 0, s1 = 0, s2 = 0;
+    T s0 = 0, s1 = 0, s2 = 0;   // a thread's sums over its few nodes of one problem, in T
     T m = 0;
+    T mean[3] = {0, 0, 0};      // subtract: the current problem's means (one division per problem change)
     int cur = -1;
     auto flush = [&]() {   // called by every thread of the CTA together
         if (cur < 0) return;
@@ -829,7 +830,7 @@ __global__ void __launch_bounds__(256) k_batch_mean3(const BProb* __restrict__ p
         if (subtract) {
             if (norm_slots) tile_max<T>(m, norm_slots, cur);
         } else {
-            double v[3] = {s0, s1, s2};
+            double v[3] = {(double)s0, (double)s1, (double)s2};
             for (int c = 0; c < 3; c++) {
                 for (int o = 16; o > 0; o >>= 1) v[c] += __shfl_xor_sync(0xffffffffu, v[c], o);
                 if (lane == 0) red[c][warp] = v[c];
@@ -849,26 +850,29 @@ __global__ void __launch_bounds__(256) k_batch_mean3(const BProb* __restrict__ p
         const BTile tl = tiles[t];
         if (tl.prob < 0) break;   // compacted list: only end markers follow (uniform over the CTA)
         if (active && !active[tl.prob]) continue;   // uniform over the CTA
+        const BProb& P = probs[tl.prob];
         if (tl.prob != cur) {
             flush();
             cur = tl.prob;
+            if (subtract) {
+                const double cnt = (double)P.L.count();
+                for (int c = 0; c < 3; c++) mean[c] = (T)(sums[cur * 3 + c] / cnt);
+            }
         }
-        const BProb& P = probs[tl.prob];
         int i, j, k;
         if (!tile_node<32, 4, 2>(tl, P.L, i, j, k)) continue;
         const long long q = P.vo + P.L.idx(i, j, k);
         if (subtract) {
-            const double cnt = (double)P.L.count();
             for (int c = 0; c < 3; c++) {
-                const T v = (T)((double)y[q + c * P.L.S] - sums[tl.prob * 3 + c] / cnt);
+                const T v = y[q + c * P.L.S] - mean[c];
                 y[q + c * P.L.S] = v;
                 const T a = fabs(v);
                 m = (a > m || a != a) ? a : m;
             }
         } else {
-            s0 += (double)y[q];
-            s1 += (double)y[q + P.L.S];
-            s2 += (double)y[q + 2 * P.L.S];
+            s0 += y[q];
+            s1 += y[q + P.L.S];
+            s2 += y[q + 2 * P.L.S];
         }
     }
     flush();

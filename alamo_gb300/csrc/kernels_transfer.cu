@@ -276,13 +276,26 @@ __global__ void k_mean3(LevelDesc L, T* __restrict__ x, double* __restrict__ sum
     const long long cnt = L.count();
     double s[3] = {0, 0, 0};
     T m = 0;
+    T mean[3] = {0, 0, 0};
+    if (subtract)
+        for (int c = 0; c < 3; c++) mean[c] = (T)(sums[c] / (double)cnt);
+    const bool small = cnt <= 0x7fffffffLL;   // 32-bit index arithmetic
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < cnt; e += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(e % L.nn[0]), j = (int)((e / L.nn[0]) % L.nn[1]),
-                  k = (int)(e / ((long long)L.nn[0] * L.nn[1]));
+        int i, j, k;
+        if (small) {
+            const int ei = (int)e;
+            i = ei % L.nn[0];
+            j = (ei / L.nn[0]) % L.nn[1];
+            k = ei / (L.nn[0] * L.nn[1]);
+        } else {
+            i = (int)(e % L.nn[0]);
+            j = (int)((e / L.nn[0]) % L.nn[1]);
+            k = (int)(e / ((long long)L.nn[0] * L.nn[1]));
+        }
         const long long q = L.idx(i, j, k);
         for (int c = 0; c < 3; c++) {
             if (subtract) {
-                const T v = (T)((double)x[c * L.S + q] - sums[c] / (double)cnt);
+                const T v = x[c * L.S + q] - mean[c];
                 x[c * L.S + q] = v;
                 const T a = fabs(v);
                 m = (a > m || a != a) ? a : m;
