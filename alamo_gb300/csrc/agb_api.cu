@@ -606,12 +606,28 @@ agb_status norm64(agb_op op, const LevelDesc& L, const double* x, double* norm)
     return AGB_OK;
 }
 
+
+// The solve's first residual.  With a zero initial guess (a fresh solve,
+// Newton's correction) r = b: A 0 = 0 holds exactly in every row (interior,
+// displacement, traction and Neumann rows alike), so the FP64 operator
+// application is skipped; b is already projected on a fully periodic box.
+agb_status initial_residual(agb_solver s, double* res0)
+{
+    agb_op op = s->op;
+    Level& v0 = op->lev[0];
+    double xn;
+    TRY(norm64(op, v0.L, s->x64, &xn));
+    if (xn != 0) return residual64(s, res0);
+    CK(cudaMemcpyAsync(v0.res64, s->b64, sizeof(double) * 3 * (size_t)v0.L.S, cudaMemcpyDeviceToDevice, op->st));
+    return norm64(op, v0.L, v0.res64, res0);
+}
+
 // MLMG::solve restated on the resident (x64, b64); FP64 throughout.
 agb_status solve_plain(agb_solver s, double tol_rel, double tol_abs, agb_solve_report* rep)
 {
     agb_op op = s->op;
     double res0, bnorm;
-    TRY(residual64(s, &res0));
+    TRY(initial_residual(s, &res0));
     TRY(norm64(op, op->lev[0].L, s->b64, &bnorm));
     const double max_norm = bnorm >= res0 ? bnorm : res0;
     const double target = std::max(tol_abs, std::max(tol_rel, 1e-16) * max_norm);
@@ -751,7 +767,7 @@ agb_status solve_mixed(agb_solver s, double tol_rel, double tol_abs, agb_solve_r
     TRY(ensure_f32(op));
     Level& v0 = op->lev[0];
     double res0, bnorm;
-    TRY(residual64(s, &res0));
+    TRY(initial_residual(s, &res0));
     TRY(norm64(op, v0.L, s->b64, &bnorm));
     const double max_norm = bnorm >= res0 ? bnorm : res0;
     const double target = std::max(tol_abs, std::max(tol_rel, 1e-16) * max_norm);

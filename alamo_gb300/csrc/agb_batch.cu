@@ -119,6 +119,12 @@ struct agb_batch_s {
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     cudaGraphExec_t g64 = nullptr, g32 = nullptr;
     long long g64_k = 0, g32_k = 0;
+    // per-problem GCR over the FP32 cycle (params.krylov > 0): directions,
+    // their images, per-problem scalars, one graph per number of stored directions
+    std::vector<float*> kZ, kW;
+    double *kdots = nullptr, *kd2 = nullptr;
+    std::vector<cudaGraphExec_t> gk;
+    std::vector<long long> gk_k;
     long long compact_tiles = -1;   // level-0 tiles in the compacted lists (-1: not built)
     std::vector<int> compact_mask;
     int grid = 152 * 4;
@@ -455,20 +461,30 @@ template <typename T> void project(agb_batch b, const int* act, T* y, bool norms
 }
 
 // compacted: use the lists of the problems still iterating (inside the cycle graphs)
+// Stencil tiles of the finest level for all problems: the level's tuned list
+// when it covers every problem (each has a coarser level), else the full list
+// in the node-per-thread shape.
+void fine_tiles(agb_batch b, bool compacted, int* shape, const BTile** tl, int* nt)
+{
+    BLevel& v = b->lev[0];
+    bool tuned = b->tuned && !v.tS_smooth.empty();
+    for (int q = 0; tuned && q < b->np; q++) tuned = b->bottom[q] > 0;
+    *shape = tuned ? v.shape : 0;
+    *tl = tuned ? (compacted ? v.c_tS_smooth : v.d_tS_smooth) : (compacted ? v.c_t32_full : v.d_t32_full);
+    *nt = tuned ? (int)v.tS_smooth.size() : (int)v.t32_full.size();
+}
+
 template <typename T>
 agb_status residual0(agb_batch b, const int* act, const T* x, const T* rhs, T* r, bool compacted = false)
 {
     BLevel& v = b->lev[0];
     const bool sing = b->per[0] && b->per[1] && b->per[2];
     BCK(cudaMemsetAsync(b->d_norms, 0, sizeof(double) * b->np, b->st));
-    // the level's tuned tile list when it covers every problem (each has a
-    // coarser level), else the full list in the node-per-thread shape
-    bool tuned = b->tuned && !v.tS_smooth.empty();
-    for (int q = 0; tuned && q < b->np; q++) tuned = b->bottom[q] > 0;
-    const BTile* tl = tuned ? (compacted ? v.c_tS_smooth : v.d_tS_smooth) : (compacted ? v.c_t32_full : v.d_t32_full);
-    const int nt = tuned ? (int)v.tS_smooth.size() : (int)v.t32_full.size();
-    launch_batch_stencil<T>(b->st, b->sym, MODE_RESID, tuned ? v.shape : 0, b->grid, v.d_probs, tl, nt, act, b->bc,
-                            false, BArr<T>::ddw(v), x, rhs, nullptr, r, (T)0, sing ? nullptr : b->d_norms);
+    int shape, nt;
+    const BTile* tl;
+    fine_tiles(b, compacted, &shape, &tl, &nt);
+    launch_batch_stencil<T>(b->st, b->sym, MODE_RESID, shape, b->grid, v.d_probs, tl, nt, act, b->bc, false,
+                            BArr<T>::ddw(v), x, rhs, nullptr, r, (T)0, sing ? nullptr : b->d_norms);
     if (sing) project<T>(b, act, r, true, compacted);
     BCK(cudaMemcpyAsync(b->h_norms, b->d_norms, sizeof(double) * b->np, cudaMemcpyDeviceToHost, b->st));
     return AGB_OK;
@@ -495,6 +511,73 @@ template <class Fn> agb_status bcapture(agb_batch b, cudaGraphExec_t* out, long 
     const cudaError_t e2 = cudaGraphInstantiate(out, g, 0);
     cudaGraphDestroy(g);
     if (e2 != cudaSuccess) return bfail(AGB_CUDA, cudaGetErrorString(e2));
+    return AGB_OK;
+}
+
+// One GCR iteration of every problem still iterating (d_iactive), with k
+// directions stored: z = V(r) (the batched FP32 V-cycle on res32(0), which it
+// leaves unchanged), w = A z (projected on fully periodic problems), w and z
+// orthogonalised against the stored directions, and the residual minimised
+// over the new one; max |r| per problem into the norm slots (FP32 encoding).
+void gcr_iter_body(agb_batch b, int k)
+{
+    BLevel& v0 = b->lev[0];
+    const int* act = b->d_iactive;
+    const int np = b->np;
+    BEngine<float> E{b, act};
+    E.vcycle();
+    float* z = b->kZ[k];
+    float* w = b->kW[k];
+    launch_batch_vec(b->st, BV_COPY, b->grid, v0.d_probs, v0.c_t32_full, (int)v0.t32_full.size(), act, z, v0.cor32,
+                     0.0, nullptr, 1);
+    int shape, nt;
+    const BTile* tl;
+    fine_tiles(b, true, &shape, &tl, &nt);
+    launch_batch_stencil<float>(b->st, b->sym, MODE_APPLY, shape, b->grid, v0.d_probs, tl, nt, act, b->bc, false,
+                                v0.ddw32, z, nullptr, nullptr, w, 0.0f, nullptr);
+    if (b->per[0] && b->per[1] && b->per[2]) project<float>(b, act, w, false, true);
+    cudaMemsetAsync(b->kdots, 0, sizeof(double) * (size_t)np * GCR_MAX, b->st);
+    cudaMemsetAsync(b->kd2, 0, sizeof(double) * (size_t)np * 2, b->st);
+    if (k > 0) {
+        GcrVecs W, Z;
+        for (int i = 0; i < k; i++) {
+            W.v[i] = b->kW[i];
+            Z.v[i] = b->kZ[i];
+        }
+        launch_batch_multidot(b->st, b->grid, v0.d_probs, v0.c_t32_full, (int)v0.t32_full.size(), act, k, w, W,
+                              v0.dinv32, b->kdots, GCR_MAX);
+        launch_batch_gcr_orth(b->st, b->grid, v0.d_probs, v0.c_t32_full, (int)v0.t32_full.size(), act, k, b->kdots,
+                              GCR_MAX, W, Z, w, z);
+    }
+    GcrVecs P;
+    P.v[0] = w;
+    P.v[1] = v0.res32;
+    launch_batch_multidot(b->st, b->grid, v0.d_probs, v0.c_t32_full, (int)v0.t32_full.size(), act, 2, w, P,
+                          v0.dinv32, b->kd2, 2);
+    cudaMemsetAsync(b->d_norms, 0, sizeof(double) * np, b->st);
+    launch_batch_gcr_step(b->st, b->grid, v0.d_probs, v0.c_t32_full, (int)v0.t32_full.size(), act, b->kd2, w, z,
+                          b->sol32, v0.res32, b->d_norms);
+    cudaMemcpyAsync(b->h_norms, b->d_norms, sizeof(double) * np, cudaMemcpyDeviceToHost, b->st);
+}
+
+agb_status gcr_setup(agb_batch b, int m)
+{
+    BLevel& v0 = b->lev[0];
+    while ((int)b->kZ.size() < m) {
+        float *z = nullptr, *w = nullptr;
+        BTRY(b->alloc(&z, v0.nvec));
+        BTRY(b->alloc(&w, v0.nvec));
+        b->kZ.push_back(z);
+        b->kW.push_back(w);
+    }
+    if (!b->kdots) {
+        BTRY(b->alloc(&b->kdots, (size_t)b->np * GCR_MAX));
+        BTRY(b->alloc(&b->kd2, (size_t)b->np * 2));
+    }
+    b->gk.resize(m, nullptr);
+    b->gk_k.resize(m, 0);
+    for (int k = 0; k < m; k++)
+        if (!b->gk[k]) BTRY(bcapture(b, &b->gk[k], &b->gk_k[k], [&] { gcr_iter_body(b, k); }));
     return AGB_OK;
 }
 
@@ -525,6 +608,10 @@ agb_status agb_batch_create(int nprob, const int* n_cells, const double* dx, con
     for (int d = 0; d < 3; d++) b->per[d] = periodic ? (periodic[d] ? 1 : 0) : 1;
     if (params) b->p = *params;
     else agb_default_params(&b->p);
+    if (b->p.krylov < 0 || b->p.krylov > GCR_MAX) {
+        delete b;
+        return bfail(AGB_BADARG, "krylov must be in 0..16");
+    }
     if (b->p.omega > 0) b->omega = b->p.omega;
     memset(&b->bc, 0, sizeof(b->bc));
     b->n.assign(n_cells, n_cells + 3 * nprob);
@@ -555,6 +642,8 @@ agb_status agb_batch_destroy(agb_batch b)
     if (b->st) cudaStreamSynchronize(b->st);
     if (b->g64) cudaGraphExecDestroy(b->g64);
     if (b->g32) cudaGraphExecDestroy(b->g32);
+    for (cudaGraphExec_t g : b->gk)
+        if (g) cudaGraphExecDestroy(g);
     for (void* v : b->allocs) cudaFree(v);
     if (b->h_norms) cudaFreeHost(b->h_norms);
     if (b->e0) cudaEventDestroy(b->e0);
@@ -674,6 +763,8 @@ agb_status agb_batch_solve(agb_batch b, double tol_rel, double tol_abs, agb_solv
                                  b->d_iactive, b->sol32, v0.cor32, 1.0, nullptr, 1);
                 residual0<float>(b, b->d_iactive, b->sol32, b->rhs32, v0.res32, true);
             }));
+        const int m = std::min(std::max(b->p.krylov, 0), GCR_MAX);
+        if (m > 0) BTRY(gcr_setup(b, m));
         std::vector<double> scale(np, 1.0), itol(np);
         for (int outer = 0; outer < b->p.max_refine && any(b->active); outer++) {
             for (int q = 0; q < np; q++) {
@@ -693,8 +784,14 @@ agb_status agb_batch_solve(agb_batch b, double tol_rel, double tol_abs, agb_solv
             std::vector<int> slow(np, 0);
             for (int it = 0; it < b->p.inner_max_iter && any(b->iactive); it++) {
                 BTRY(compact(b, b->iactive));
-                BCK(cudaGraphLaunch(b->g32, b->st));
-                replayed += b->g32_k;
+                if (m > 0) {
+                    const int k = it % m;   // restarted when all m directions are stored
+                    BCK(cudaGraphLaunch(b->gk[k], b->st));
+                    replayed += b->gk_k[k];
+                } else {
+                    BCK(cudaGraphLaunch(b->g32, b->st));
+                    replayed += b->g32_k;
+                }
                 BCK(cudaStreamSynchronize(b->st));
                 for (int q = 0; q < np; q++) {
                     if (!b->iactive[q]) continue;

@@ -134,6 +134,18 @@ void launch_batch_mean3(cudaStream_t st, int grid, const BProb* probs, const BTi
                         const int* active, T* y, double* sums, int subtract, void* norm_slots = nullptr);
 int batch_shape_count();
 void batch_shape_dims(int shape, int dims[3]);
+// Per-problem GCR over the batched FP32 cycle (kernels_batch.cu; GcrVecs
+// and GCR_MAX as for the single-box inner GCR).  Tiles: the 32 x 4 x 2 lists.
+struct GcrVecs;
+void launch_batch_multidot(cudaStream_t st, int grid, const BProb* probs, const BTile* tiles, int ntiles,
+                           const int* active, int k, const float* x, const GcrVecs& V, const float* d, double* out,
+                           int stride);
+void launch_batch_gcr_orth(cudaStream_t st, int grid, const BProb* probs, const BTile* tiles, int ntiles,
+                           const int* active, int k, const double* beta, int stride, const GcrVecs& W,
+                           const GcrVecs& Z, float* w, float* z);
+void launch_batch_gcr_step(cudaStream_t st, int grid, const BProb* probs, const BTile* tiles, int ntiles,
+                           const int* active, const double* dots, float* w, float* z, float* c, float* r,
+                           void* norm_slots);
 // whether stencil tile shape `shape` serves batches of this symmetry and periodicity
 bool batch_shape_ok(int shape, int sym, const int per[3]);
 

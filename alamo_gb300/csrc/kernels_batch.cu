@@ -976,6 +976,185 @@ void launch_batch_vec(cudaStream_t st, int op, int grid, const BProb* probs, con
     count_launch();
 }
 
+// ---------------------------------------------------------------------------
+// Per-problem GCR over the batched FP32 cycle (the single-box inner_gcr32 on
+// every problem at once).  Tiles are the 32 x 4 x 2 lists, ordered by
+// problem; a CTA flushes its sums to the problem's slots when its tiles move
+// to another problem.  Inner products are weighted by d^2 (d = 1/diag).
+// ---------------------------------------------------------------------------
+
+// out[p * stride + i] += sum over problem p's nodes of x v_i d^2, i < K
+template <int K>
+__global__ void __launch_bounds__(256) k_batch_multidot(const BProb* __restrict__ probs,
+                                                        const BTile* __restrict__ tiles, int ntiles,
+                                                        const int* __restrict__ active, const float* __restrict__ x,
+                                                        GcrVecs V, const float* __restrict__ d,
+                                                        double* __restrict__ out, int stride)
+{
+    __shared__ double red[K][8];
+    float acc[K];
+#pragma unroll
+    for (int i = 0; i < K; i++) acc[i] = 0;
+    int cur = -1;
+    auto flush = [&]() {   // every thread of the CTA together
+        if (cur < 0) return;
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+        for (int i = 0; i < K; i++) {
+            double a = (double)acc[i];
+            for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+            if (lane == 0) red[i][warp] = a;
+            acc[i] = 0;
+        }
+        __syncthreads();
+        if (threadIdx.x < K) {
+            double t = 0;
+            for (int w = 0; w < 8; w++) t += red[threadIdx.x][w];
+            atomicAdd(out + (long long)cur * stride + threadIdx.x, t);
+        }
+        __syncthreads();
+    };
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const BTile tl = tiles[t];
+        if (tl.prob < 0) break;   // compacted list: only end markers follow (uniform over the CTA)
+        if (active && !active[tl.prob]) continue;
+        if (tl.prob != cur) {
+            flush();
+            cur = tl.prob;
+        }
+        const BProb& P = probs[tl.prob];
+        int i, j, k;
+        if (!tile_node<32, 4, 2>(tl, P.L, i, j, k)) continue;
+        const long long q = P.vo + P.L.idx(i, j, k);
+        for (int c = 0; c < 3; c++) {
+            const long long e = q + c * P.L.S;
+            const float dd = d[e];
+            const float xw = x[e] * dd * dd;
+#pragma unroll
+            for (int m = 0; m < K; m++) acc[m] += xw * V.v[m][e];
+        }
+    }
+    flush();
+}
+
+// w -= sum_i beta_i(p) W_i, z -= sum_i beta_i(p) Z_i on problem p's nodes, i < K
+template <int K>
+__global__ void __launch_bounds__(256) k_batch_gcr_orth(const BProb* __restrict__ probs,
+                                                        const BTile* __restrict__ tiles, int ntiles,
+                                                        const int* __restrict__ active,
+                                                        const double* __restrict__ beta, int stride, GcrVecs W,
+                                                        GcrVecs Z, float* __restrict__ w, float* __restrict__ z)
+{
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const BTile tl = tiles[t];
+        if (tl.prob < 0) break;
+        if (active && !active[tl.prob]) continue;
+        const BProb& P = probs[tl.prob];
+        int i, j, k;
+        if (!tile_node<32, 4, 2>(tl, P.L, i, j, k)) continue;
+        float bb[K];
+#pragma unroll
+        for (int m = 0; m < K; m++) bb[m] = (float)beta[(long long)tl.prob * stride + m];
+        const long long q = P.vo + P.L.idx(i, j, k);
+        for (int c = 0; c < 3; c++) {
+            const long long e = q + c * P.L.S;
+            float tw = w[e], tz = z[e];
+#pragma unroll
+            for (int m = 0; m < K; m++) {
+                tw -= bb[m] * W.v[m][e];
+                tz -= bb[m] * Z.v[m][e];
+            }
+            w[e] = tw;
+            z[e] = tz;
+        }
+    }
+}
+
+// with ww = dots[2p], rw = dots[2p+1]: (w, z) scaled to unit norm,
+// c += (rw / ww) z, r -= (rw / ww) w, max |r| per problem -> norm_slots
+__global__ void __launch_bounds__(256) k_batch_gcr_step(const BProb* __restrict__ probs,
+                                                        const BTile* __restrict__ tiles, int ntiles,
+                                                        const int* __restrict__ active,
+                                                        const double* __restrict__ dots, float* __restrict__ w,
+                                                        float* __restrict__ z, float* __restrict__ c,
+                                                        float* __restrict__ r, void* norm_slots)
+{
+    float nrm = 0;
+    int cur = -1;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const BTile tl = tiles[t];
+        if (tl.prob < 0) break;
+        if (active && !active[tl.prob]) continue;
+        if (tl.prob != cur) {
+            if (cur >= 0) tile_max<float>(nrm, norm_slots, cur);
+            nrm = 0;
+            cur = tl.prob;
+        }
+        const BProb& P = probs[tl.prob];
+        int i, j, k;
+        if (!tile_node<32, 4, 2>(tl, P.L, i, j, k)) continue;
+        const double ww = dots[2 * tl.prob], rw = dots[2 * tl.prob + 1];
+        const float inv = ww > 0 ? (float)(1.0 / sqrt(ww)) : 0.0f;
+        const float a = ww > 0 ? (float)(rw / sqrt(ww)) : 0.0f;
+        const long long q = P.vo + P.L.idx(i, j, k);
+        for (int cc = 0; cc < 3; cc++) {
+            const long long e = q + cc * P.L.S;
+            const float wu = w[e] * inv, zu = z[e] * inv;
+            w[e] = wu;
+            z[e] = zu;
+            c[e] += a * zu;
+            const float rn = r[e] - a * wu;
+            r[e] = rn;
+            const float v = fabsf(rn);
+            nrm = (v > nrm || v != v) ? v : nrm;
+        }
+    }
+    if (cur >= 0) tile_max<float>(nrm, norm_slots, cur);
+}
+
+void launch_batch_multidot(cudaStream_t st, int grid, const BProb* probs, const BTile* tiles, int ntiles,
+                           const int* active, int k, const float* x, const GcrVecs& V, const float* d, double* out,
+                           int stride)
+{
+    switch (k) {
+#define K_(K)                                                                                                 \
+    case K:                                                                                                   \
+        k_batch_multidot<K><<<fit_grid((const void*)k_batch_multidot<K>, grid, st), 256, 0, st>>>(            \
+            probs, tiles, ntiles, active, x, V, d, out, stride);                                              \
+        break;
+        K_(1) K_(2) K_(3) K_(4) K_(5) K_(6) K_(7) K_(8) K_(9) K_(10) K_(11) K_(12) K_(13) K_(14) K_(15) K_(16)
+#undef K_
+    default: return;
+    }
+    count_launch();
+}
+
+void launch_batch_gcr_orth(cudaStream_t st, int grid, const BProb* probs, const BTile* tiles, int ntiles,
+                           const int* active, int k, const double* beta, int stride, const GcrVecs& W,
+                           const GcrVecs& Z, float* w, float* z)
+{
+    switch (k) {
+#define K_(K)                                                                                                 \
+    case K:                                                                                                   \
+        k_batch_gcr_orth<K><<<fit_grid((const void*)k_batch_gcr_orth<K>, grid, st), 256, 0, st>>>(            \
+            probs, tiles, ntiles, active, beta, stride, W, Z, w, z);                                          \
+        break;
+        K_(1) K_(2) K_(3) K_(4) K_(5) K_(6) K_(7) K_(8) K_(9) K_(10) K_(11) K_(12) K_(13) K_(14) K_(15) K_(16)
+#undef K_
+    default: return;
+    }
+    count_launch();
+}
+
+void launch_batch_gcr_step(cudaStream_t st, int grid, const BProb* probs, const BTile* tiles, int ntiles,
+                           const int* active, const double* dots, float* w, float* z, float* c, float* r,
+                           void* norm_slots)
+{
+    grid = fit_grid((const void*)k_batch_gcr_step, grid, st);
+    k_batch_gcr_step<<<grid, 256, 0, st>>>(probs, tiles, ntiles, active, dots, w, z, c, r, norm_slots);
+    count_launch();
+}
+
 void launch_batch_bottom(cudaStream_t st, int sym, int fp32, const BProb* probs, const int* plist, int np,
                          const int* active, const BCTable& bc, bool uniform, const void* ddw, const double* diag,
                          void* cor, const void* res, double* work, int maxiter, double tol_rel, double tol_abs, int nub,

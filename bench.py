@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cycle", default="F", choices=["F", "V"])
     ap.add_argument("--krylov", type=int, default=8,
-                    help="c2: stored directions of the flexible GCR over the FP32 cycle (0: the FP32 cycles alone)")
+                    help="c2, rve: stored directions of the flexible GCR over the FP32 cycle (0: the FP32 cycles alone)")
     ap.add_argument("--workload", default="c2", choices=["c2", "rve", "learned"],
                     help="c2: the 257^3 polycrystal (default); rve: batched periodic RVEs; learned: the learned "
                          "correction trained on 64^3 RVEs and evaluated at 128^3 and 256^3")
@@ -321,7 +321,8 @@ def run_rve(args, dist):
     probs = [M.rve_params(q) for q in range(nprob)]
     sizes = [(p[0],) * 3 for p in probs]
     nodes = sum((n + 1) ** 3 for n, _, _ in probs)
-    bt = Batch(sizes, precision=1 if args.precision == "mixed" else 0)
+    bt = Batch(sizes, precision=1 if args.precision == "mixed" else 0,
+               krylov=args.krylov if args.precision == "mixed" else 0)
     for q in range(nprob):
         _, ddw, _ = M.rve_problem_device(q)
         bt.SetModel(q, ddw)

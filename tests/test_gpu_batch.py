@@ -138,3 +138,29 @@ def test_single_box_periodic_gcr(gpu_lib):
     assert projected_residual_ratio(g, ddw, x, rhs, n) <= 1e-9 * 1.00001
     err = np.abs(x - xo).max() / np.abs(xo).max()
     assert err < 1e-6, err
+
+
+def test_batch_gcr_matches_oracle(gpu_lib):
+    """The batched mixed solve with a per-problem GCR over the FP32 V-cycle
+    (krylov = 8): every problem converges to the oracle's solution, in no more
+    cycles than the FP32 cycles alone need."""
+    from alamo_gb300.batch import Batch
+    sizes = [8, 12, 16, 24]
+    probs = small_rves(sizes, seed=13)
+    cyc = {}
+    for kr in (0, 8):
+        bt = Batch([(n, n, n) for n in sizes], precision=1, krylov=kr)
+        for q, (n, ddw, F0) in enumerate(probs):
+            bt.SetModel(q, ddw)
+        bt.SetEigenstrain(np.stack([p[2] for p in probs]))
+        assert bt.solve(1e-8, 0.0).status == 0
+        cyc[kr] = [bt.reports[q].iterations for q in range(len(sizes))]
+        if kr:
+            for q, (n, ddw, F0) in enumerate(probs):
+                g, rhs, xo, rep_o = oracle_solution(n, ddw, F0, 1e-8)
+                u = bt.solution(q)
+                assert projected_residual_ratio(g, ddw, u, rhs, n) <= 1e-8 * 1.00001, q
+                assert np.abs(u - xo).max() / np.abs(xo).max() < 1e-6, q
+        bt.close()
+    print("cycles per problem: alone %s, under GCR %s" % (cyc[0], cyc[8]))
+    assert max(cyc[8]) <= max(cyc[0])
