@@ -26,17 +26,15 @@ namespace agb {
 // not resident from the start runs its share of the tiles after a resident
 // one has finished all of its own, which adds a second wave; so each launch is
 // trimmed to the CTAs of that kernel (256 threads) that fit on the device at
-// once.  Queried once per kernel, outside stream capture (while capturing, an
-// unqueried kernel keeps `grid`).
-static int fit_grid(const void* kernel, int grid, cudaStream_t st)
+// once.  Queried once per kernel (the occupancy query is no stream operation,
+// so it may also run while a graph is being captured).
+static int fit_grid(const void* kernel, int grid, cudaStream_t)
 {
     static std::mutex mu;
     static std::unordered_map<const void*, int> cache;
     std::lock_guard<std::mutex> lock(mu);
     auto it = cache.find(kernel);
     if (it != cache.end()) return std::min(grid, it->second);
-    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return grid;
     int dev = 0, sms = 0, per = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, 256, 0) != cudaSuccess || per < 1 || sms < 1)
