@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <mutex>
 #include <unordered_map>
 
@@ -355,6 +356,158 @@ __global__ void __launch_bounds__(256) k_batch_march(const BProb* __restrict__ p
         }
     }
     if (MODE == MODE_RESID && norm_slots && cur >= 0) tile_max<T>(nrm, norm_slots, cur);
+}
+
+// ---------------------------------------------------------------------------
+// The FP32 marching tile kernel with asynchronous plane copies.  Same tiles,
+// halo wrap and per-node arithmetic as k_batch_march, but every thread
+// copies its halo values of a plane global -> shared with 4-byte cp.async
+// (the wrapped halo rows are not contiguous), three planes ahead of the
+// compute: u in a ring of 4 planes (k-1, k, k+1 and plane k+2 in flight),
+// moduli in a ring of 3 (k, k+1, and k+2 in flight); one commit group per
+// plane.  The copies of plane k+3 are issued as soon as plane k is done.
+// ---------------------------------------------------------------------------
+template <int SYM> struct BPipeSmem {
+    static constexpr int NC = NCoef<SYM>::value;
+    float u[4][3][BM_HALO];
+    float c[3][NC][BM_HALO];
+};
+
+template <int SYM> struct BPipeAcc {
+    const BPipeSmem<SYM>* s;
+    int h;
+    int um, u0, up, c0, cp;
+    float cm[NCoef<SYM>::value];
+    __device__ __forceinline__ float u(int p, int di, int dj, int dk) const
+    {
+        const int r = dk < 0 ? um : (dk > 0 ? up : u0);
+        return s->u[r][p][h + di + BMH_X * dj];
+    }
+    __device__ __forceinline__ float C(int m, int di, int dj, int dk) const
+    {
+        if (dk < 0) return cm[m];
+        if (dk > 0) return s->c[cp][m][h];
+        return s->c[c0][m][h + di + BMH_X * dj];
+    }
+};
+
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem)
+{
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+template <int SYM, int MODE>
+__global__ void __launch_bounds__(256) k_batch_pipe(const BProb* __restrict__ probs, const BTile* __restrict__ tiles,
+                                                    int ntiles, const int* __restrict__ active, int uniform,
+                                                    const float* __restrict__ ddw, const float* __restrict__ x,
+                                                    const float* __restrict__ b, const float* __restrict__ dinv,
+                                                    float* __restrict__ out, float omega, void* norm_slots)
+{
+    __shared__ __align__(16) BPipeSmem<SYM> s;
+    constexpr int NC = NCoef<SYM>::value;
+    const int tid = threadIdx.x, tx = tid % BM_X, ty = tid / BM_X;
+    float nrm = 0;
+    int cur = -1;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const BTile tl = tiles[t];
+        if (tl.prob < 0) break;   // compacted list: only end markers follow (uniform over the CTA)
+        if (active && !active[tl.prob]) continue;
+        if (MODE == MODE_RESID && norm_slots && tl.prob != cur) {
+            if (cur >= 0) tile_max<float>(nrm, norm_slots, cur);
+            nrm = 0;
+            cur = tl.prob;
+        }
+        const BProb& P = probs[tl.prob];
+        const LevelDesc& L = P.L;
+        const Geo<float> g = geo_of<float>(P);
+        const long long S = L.S, plane = (long long)L.P * L.nn[1];
+        const float* xp = x + P.vo;
+        const float* cq = ddw + P.co;
+        const int i0 = tl.bx * BM_X, j0 = tl.by * BM_Y, k0 = tl.bz * BM_Z;
+        const int k1 = min(k0 + BM_Z, L.n[2]);
+        const int i = i0 + tx, j = j0 + ty;
+        const bool mine = i < L.n[0] && j < L.n[1];
+        long long hoff[BM_PER_THREAD];
+#pragma unroll
+        for (int q = 0; q < BM_PER_THREAD; q++) {
+            const int e = min(tid + 256 * q, BM_HALO - 1);
+            hoff[q] = (long long)pwrap(i0 - 1 + e % BMH_X, L.n[0]) +
+                      (long long)L.P * pwrap(j0 - 1 + e / BMH_X, L.n[1]);
+        }
+        // copies of plane kk: u into ring slot (kk - k0 + 1) % 4, moduli (when
+        // with_c) into (kk - k0) % 3; one commit group (empty past the chunk)
+        auto issue = [&](int kk, bool with_c) {
+            if (kk <= k1) {
+                const long long pk = plane * pwrap(kk, L.n[2]);
+                const int ur = (kk - k0 + 1) & 3, cr = (kk - k0 + 3) % 3;
+#pragma unroll
+                for (int q = 0; q < BM_PER_THREAD; q++) {
+                    const int e = tid + 256 * q;
+                    if (e < BM_HALO) {
+#pragma unroll
+                        for (int c = 0; c < 3; c++) cp_async4(&s.u[ur][c][e], xp + c * S + hoff[q] + pk);
+                        if (with_c) {
+#pragma unroll
+                            for (int m = 0; m < NC; m++) cp_async4(&s.c[cr][m][e], cq + m * S + hoff[q] + pk);
+                        }
+                    }
+                }
+            }
+            cp_commit();
+        };
+        BPipeAcc<SYM> acc;
+        acc.s = &s;
+        acc.h = (tx + 1) + BMH_X * (ty + 1);
+        {
+            const long long p = (long long)min(i, L.n[0] - 1) + (long long)L.P * min(j, L.n[1] - 1) +
+                                plane * pwrap(k0 - 1, L.n[2]);
+#pragma unroll
+            for (int m = 0; m < NC; m++) acc.cm[m] = __ldg(cq + m * S + p);
+        }
+        issue(k0 - 1, false);
+        issue(k0, true);
+        issue(k0 + 1, true);
+        issue(k0 + 2, true);
+        for (int k = k0; k < k1; k++) {
+            cp_wait1();   // every group but the newest (plane k+2) has landed
+            __syncthreads();
+            const int it = k - k0;
+            acc.um = it & 3;
+            acc.u0 = (it + 1) & 3;
+            acc.up = (it + 2) & 3;
+            acc.c0 = it % 3;
+            acc.cp = (it + 1) % 3;
+            if (mine) {
+                float f[3];
+                interior_row<float, SYM>(acc, g, uniform != 0, f);
+                const long long q0 = P.vo + L.idx(i, j, k);
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    const long long o = q0 + c * S;
+                    if (MODE == MODE_APPLY) out[o] = f[c];
+                    else if (MODE == MODE_RESID) {
+                        const float r = b[o] - f[c];
+                        out[o] = r;
+                        const float a = fabsf(r);
+                        nrm = (a > nrm || a != a) ? a : nrm;
+                    } else {
+                        out[o] = s.u[acc.u0][c][acc.h] + omega * ((b[o] - f[c]) * dinv[o]);
+                    }
+                }
+            }
+#pragma unroll
+            for (int m = 0; m < NC; m++) acc.cm[m] = s.c[acc.c0][m][acc.h];
+            __syncthreads();
+            issue(k + 3, true);   // into the slots of u(k-1) and moduli(k)
+        }
+        cp_wait0();
+        __syncthreads();
+    }
+    if (MODE == MODE_RESID && norm_slots && cur >= 0) tile_max<float>(nrm, norm_slots, cur);
 }
 
 // Full weighting (restriction) or trilinear prolongation between the levels of
@@ -892,6 +1045,17 @@ template void launch_batch_mean3<float>(cudaStream_t, int, const BProb*, const B
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
+// The FP32 marching shape uses the asynchronous-copy kernel unless
+// AGB_BATCH_PIPE=0 (then the register-prefetch kernel, as for FP64).
+static bool batch_pipe_enabled()
+{
+    static const bool v = [] {
+        const char* e = getenv("AGB_BATCH_PIPE");
+        return !(e && e[0] == '0');
+    }();
+    return v;
+}
+
 template <typename T, int SYM, int MODE>
 static void bst_shape(cudaStream_t st, int shape, int grid, const BProb* probs, const BTile* tiles, int ntiles,
                       const int* active, const BCTable& bc, bool uniform, const T* ddw, const T* x, const T* b,
@@ -905,6 +1069,16 @@ static void bst_shape(cudaStream_t st, int shape, int grid, const BProb* probs, 
     // (batch_shape_ok)
     if constexpr (SYM == SYM_ISO) {
         if (shape == kMarchShape) {
+            if constexpr (sizeof(T) == 4) {
+                if (batch_pipe_enabled()) {
+                    grid = fit_grid((const void*)k_batch_pipe<SYM, MODE>, grid, st);
+                    k_batch_pipe<SYM, MODE><<<grid, 256, 0, st>>>(probs, tiles, ntiles, active, uniform ? 1 : 0,
+                                                                  (const float*)ddw, (const float*)x, (const float*)b,
+                                                                  (const float*)dinv, (float*)out, (float)omega, norm);
+                    count_launch();
+                    return;
+                }
+            }
             grid = fit_grid((const void*)k_batch_march<T, SYM, MODE>, grid, st);
             k_batch_march<T, SYM, MODE><<<grid, 256, 0, st>>>(probs, tiles, ntiles, active, uniform ? 1 : 0, ddw, x, b,
                                                               dinv, out, omega, norm);
