@@ -323,6 +323,62 @@ agb_status ensure_f32(agb_op op)
     return AGB_OK;
 }
 
+agb_status prepare(agb_op op);
+
+// prepareForSolve for the mixed solve.  Its FP32 cycles read the FP32
+// hierarchy only, so that is built in FP32 from the finest FP64 moduli:
+// coefficients averaged and diagonals computed in FP32 (in FP64 those passes
+// take ~14 ms at 257^3 on GB300, whose FP64 rate they are bound by).  The
+// bottom level's FP64 moduli (converted), diagonal and dense operator are made
+// as well, for the bottom solve reads those.  The finest level's FP64 moduli
+// (SetModel) serve the FP64 residuals.  The FP64 hierarchy of the other
+// levels is left stale (prepared = false) until an FP64 consumer calls
+// prepare().
+agb_status prepare_mixed(agb_op op)
+{
+    if (!op->model_set) return fail(AGB_STATE, "SetModel must be called before the operator is used");
+    if (!op->bc_set) return fail(AGB_STATE, "SetBC must be called before the operator is used");
+    for (auto& lv : op->lev) {
+        const size_t n3 = 3 * (size_t)lv.L.S;
+        if (!lv.ddw32) TRY(op->alloc(&lv.ddw32, op->nc * (size_t)lv.L.S));
+        if (!lv.dinv32) TRY(op->alloc(&lv.dinv32, n3));
+        if (!lv.cor32) {
+            TRY(op->alloc(&lv.cor32, n3));
+            TRY(op->alloc(&lv.res32, n3));
+            TRY(op->alloc(&lv.rescor32, n3));
+            TRY(op->alloc(&lv.hold32, n3));
+            TRY(op->alloc(&lv.tmp32, n3));
+        }
+    }
+    const size_t nl = op->lev.size();
+    launch_convert<float, double>(op->st, op->lev[0].L, op->nc, op->lev[0].ddw64, op->lev[0].ddw32, 1.0);
+    for (size_t l = 1; l < nl; l++)
+        launch_average_ddw<float>(op->st, op->lev[l - 1].L, op->lev[l].L, op->lev[l - 1].ddw32, op->lev[l].ddw32,
+                                  op->nc);
+    for (auto& lv : op->lev) {
+        launch_diagonal<float>(op->st, op->sym, lv.L, op->bc, lv.ddw32, lv.dinv32);
+        launch_recip_inplace(op->st, lv.L, 3, lv.dinv32);
+    }
+    Level& bl = op->lev[nl - 1];
+    if (nl > 1) launch_convert<double, float>(op->st, bl.L, op->nc, bl.ddw32, bl.ddw64, 1.0);
+    launch_diagonal<double>(op->st, op->sym, bl.L, op->bc, bl.ddw64, bl.diag64);
+    launch_recip<double>(op->st, bl.L, 3, bl.diag64, bl.dinv64);
+    if (op->bottom_A)
+        launch_bottom_assemble(op->st, op->sym, bl.L, op->bc, op->uniform, bl.ddw64, op->bottom_A);
+    CK(cudaGetLastError());
+    op->prepared = false;
+    op->f32_ready = true;
+    return AGB_OK;
+}
+
+// MLMG::solve -> prepareForSolve on every call, for the solver's precision
+agb_status prepare_for_solve(agb_solver s)
+{
+    agb_op op = s->op;
+    op->prepared = false;
+    return s->p.precision == AGB_PREC_MIXED ? prepare_mixed(op) : prepare(op);
+}
+
 // averageDownCoeffs + Diagonal(true) for every level (Operator.cpp:253-260)
 agb_status prepare(agb_op op)
 {
@@ -1215,8 +1271,7 @@ agb_status agb_solve(agb_solver s, double* sol, const double* rhs, double tol_re
     const long long k0 = launch_counter();
     s->replayed = 0;
     CK(cudaEventRecord(op->e0, op->st));
-    op->prepared = false;   // MLMG::solve -> prepareForSolve on every call
-    TRY(prepare(op));
+    TRY(prepare_for_solve(s));
     TRY((upload<double, double>(op, op->lev[0].L, 3, false, sol, mem, s->x64)));
     TRY((upload<double, double>(op, op->lev[0].L, 3, false, rhs, mem, s->b64)));
     agb_status st = solve_resident(s, tol_rel, tol_abs, &rep);
@@ -1473,8 +1528,7 @@ agb_status agb_newton_solve(agb_solver s, const double* F0, double* u, const dou
     const long long k0 = launch_counter();
     s->replayed = 0;
     CK(cudaEventRecord(op->e0, op->st));
-    op->prepared = false;   // MLMG::solve -> prepareForSolve on every call
-    TRY(prepare(op));
+    TRY(prepare_for_solve(s));
     TRY(load_F0(op, F0, mem, &dF0));
     agb_status st = kept(op, &op->nw_dw, 9 * (size_t)v.L.S);
     if (st == AGB_OK) st = kept(op, &op->nw_u0, 3 * (size_t)v.L.S);

@@ -184,6 +184,8 @@ template <typename TD, typename TS>
 void launch_export(cudaStream_t st, const LevelDesc& L, int ncomp, const TS* src, TD* dst, bool aos, int k0, int kc,
                    bool chunk);
 void launch_axpy_mixed(cudaStream_t st, const LevelDesc& L, int ncomp, double* y, const float* x, double a);
+// d <- 1/d (FP32, in place; zeros stay zero)
+void launch_recip_inplace(cudaStream_t st, const LevelDesc& L, int ncomp, float* d);
 // Inner FP32 GCR (kernels_transfer.cu): up to GCR_MAX stored directions.
 constexpr int GCR_MAX = 16;
 struct GcrVecs {

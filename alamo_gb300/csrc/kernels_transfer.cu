@@ -260,6 +260,13 @@ __global__ void k_axpy_mixed(long long n, double* __restrict__ y, const float* _
         y[e] += a * (double)x[e];
 }
 
+// d <- 1/d in place (0 stays 0: padding)
+__global__ void k_recip_inplace(long long n, float* __restrict__ d)
+{
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
+        d[e] = d[e] != 0.0f ? 1.0f / d[e] : 0.0f;
+}
+
 template <typename TD>
 __global__ void k_recip(long long n, const double* __restrict__ d, TD* __restrict__ r)
 {
@@ -549,6 +556,13 @@ void launch_gcr_step(cudaStream_t st, long long n, const double* dots, float* w,
                      void* slot)
 {
     k_gcr_step<<<blocks_1d(n), 256, 0, st>>>(n, dots, w, z, c, r, slot);
+    count_launch();
+}
+
+void launch_recip_inplace(cudaStream_t st, const LevelDesc& L, int ncomp, float* d)
+{
+    const long long n = (long long)ncomp * L.S;
+    k_recip_inplace<<<blocks_1d(n), 256, 0, st>>>(n, d);
     count_launch();
 }
 
