@@ -1536,9 +1536,16 @@ agb_status agb_newton_solve(agb_solver s, const double* F0, double* u, const dou
     u0 = op->nw_u0;
     if (st == AGB_OK) st = upload<double, double>(op, v.L, 3, false, u, mem, u0);
     if (st == AGB_OK) st = upload<double, double>(op, v.L, 3, false, b, mem, v.rescor64);
+    double unorm = 1.0;
+    if (st == AGB_OK && !dF0) st = norm64(op, v.L, u0, &unorm);
     if (st == AGB_OK) {
-        // Newton.H:323: rhs from the current u; Linear::solve for dsol from 0
-        launch_newton_rhs(op->st, op->sym, v.L, op->bc, v.ddw64, dF0, u0, v.rescor64, s->b64, dw);
+        // Newton.H:323: rhs from the current u; Linear::solve for dsol from 0.
+        // Without an eigenstrain and from u = 0, DW = C : grad 0 = 0 and every
+        // row of div DW and of the BC rows is exactly 0: rhs = b.
+        if (!dF0 && unorm == 0.0)
+            cudaMemcpyAsync(s->b64, v.rescor64, sizeof(double) * 3 * (size_t)v.L.S, cudaMemcpyDeviceToDevice, op->st);
+        else
+            launch_newton_rhs(op->st, op->sym, v.L, op->bc, v.ddw64, dF0, u0, v.rescor64, s->b64, dw);
         cudaMemsetAsync(s->x64, 0, sizeof(double) * 3 * (size_t)v.L.S, op->st);
         if (cudaGetLastError() != cudaSuccess) st = fail(AGB_CUDA, "newton rhs launch failed");
     }
