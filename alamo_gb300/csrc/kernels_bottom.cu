@@ -358,7 +358,7 @@ __global__ void k_bottom_assemble(LevelDesc L, BCTable bc, Geo<double> g, int un
 // partials in warp order (so all threads hold the same value and take the
 // same branches).  Reductions that need no value in between share a barrier:
 // (max|r|, rh.r) at the end of an iteration, (t.t, t.s), and the publication
-// of s with max|s|.  A x sums over j in ascending order, as k_bottom's rows do.
+// of s with max|s|.  A x is summed as four interleaved partial sums.
 enum { RED_SUM = 0, RED_MAX = 1 };
 
 template <typename R> struct BlockRed {
@@ -411,12 +411,22 @@ __device__ void dense_bottom_block(const LevelDesc& L, const R* __restrict__ A, 
     const R eps_rel = (R)eps_rel_d, eps_abs = (R)eps_abs_d, omega = (R)omega_d;
     const bool sing = L.singular();
     BlockRed<R> br{red, 0};
-    // y = A x for the vector published in xs
+    // y = A x for the vector published in xs: four partial sums over j = 4t + s,
+    // so the loads of the next columns overlap the multiply-adds
     auto product = [&]() -> R {
-        R y = 0;
-        if (ok)
-            for (int j = 0; j < nu; j++) y += A[j * nu + q] * xs[j];
-        return y;
+        R y0 = 0, y1 = 0, y2 = 0, y3 = 0;
+        if (ok) {
+            int j = 0;
+#pragma unroll 2
+            for (; j + 3 < nu; j += 4) {
+                y0 += A[j * nu + q] * xs[j];
+                y1 += A[(j + 1) * nu + q] * xs[j + 1];
+                y2 += A[(j + 2) * nu + q] * xs[j + 2];
+                y3 += A[(j + 3) * nu + q] * xs[j + 3];
+            }
+            for (; j < nu; j++) y0 += A[j * nu + q] * xs[j];
+        }
+        return (y0 + y1) + (y2 + y3);
     };
     auto publish = [&](R x) {
         if (ok) xs[q] = x;

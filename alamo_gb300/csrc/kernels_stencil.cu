@@ -509,7 +509,7 @@ int march_min_cells()
 {
     static int v = [] {
         const char* s = getenv("AGB_MARCH_MIN_CELLS");
-        return s ? atoi(s) : 128;
+        return s ? atoi(s) : 64;
     }();
     return v;
 }
