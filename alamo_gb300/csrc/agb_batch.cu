@@ -5,8 +5,10 @@
 //
 // Per problem the algorithm is the single-box solver's (MLMG V-cycles with
 // 2+2 Fsmooth, BiCGStab bottom; FP32 cycles inside FP64 iterative refinement
-// when params.precision == AGB_PREC_MIXED), with the bottom level of each
-// problem where its own coarsening stops.  Problems that have converged are
+// when params.precision == AGB_PREC_MIXED, and with params.krylov > 0 a
+// flexible GCR of each problem over the FP32 V-cycle inside each
+// refinement), with the bottom level of each problem where its own coarsening
+// stops.  Problems that have converged are
 // masked out of the remaining launches.  The stencil tile shape of every
 // level is chosen by timing the candidate shapes on the batch's own data at
 // the first solve (autotune), and kept for the following solves.

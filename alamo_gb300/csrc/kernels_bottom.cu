@@ -274,12 +274,12 @@ __global__ void __launch_bounds__(BOT_THREADS) k_bottom(LevelDesc L, BCTable bc,
 // (3 x nodes; 81 for the 3^3-node level of a 2^k-cell box) its operator is
 // assembled once per solve as a dense matrix, column j = A e_j evaluated with
 // the same per-node rows (stencil.cuh), and the bottom solve runs the same
-// BiCGStab + smoothing as k_bottom with dense products in one warp: no
-// barrier between warps, and the operator read from shared memory instead of
-// re-evaluating every stencil row.  Results equal k_bottom's up to the
-// summation order of A x.
+// BiCGStab + smoothing as k_bottom with dense products, one thread per
+// unknown, the operator read from shared memory instead of re-evaluating
+// every stencil row.  Results equal k_bottom's up to the summation order of
+// A x and of the dot products.
 // ---------------------------------------------------------------------------
-constexpr int DENSE_MAX = 128;   // unknowns; 4 per lane of one warp
+constexpr int DENSE_MAX = 128;   // unknowns (one thread each)
 
 // Unknown q = c * cnt + e, e = i + nn0 * (j + nn1 * k) the node's place in the
 // level's node enumeration.

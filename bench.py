@@ -369,9 +369,9 @@ def run_rve(args, dist):
 
 
 def run_learned(args, dist):
-    """Learned correction (SURVEY configuration C5): train on 64^3 periodic
-    RVEs, evaluate on unseen 128^3 and 256^3 RVEs against plain FP64
-    multigrid, FP32-in-FP64 multigrid and V-cycle GCR (the ablation)."""
+    """Learned correction: train on 64^3 periodic RVEs, evaluate on unseen
+    128^3 and 256^3 RVEs against plain FP64 multigrid, FP32-in-FP64
+    multigrid and V-cycle GCR (the ablation)."""
     import numpy as np
     import torch
     from alamo_gb300 import microstructure as M
@@ -419,7 +419,7 @@ def run_learned(args, dist):
     line = {"metric": "learned correction: solve ms at 128^3 / 256^3 periodic RVEs (trained at 64^3)",
             "value": out["256^3"]["gcr_v_learned"]["ms"] / 1000.0, "unit": "s", "n_gpus": 1, "steps": 2,
             "warmup": 0, "higher_is_better": False, "dtype": "bf16 net + f32/f64 solve",
-            "data": "synthetic (seeded RVEs)", "config": {"workload": "C5: net trained on 8 samples of 64^3 RVEs"},
+            "data": "synthetic (seeded RVEs)", "config": {"workload": "learned correction: net trained on 8 samples of 64^3 RVEs, evaluated at 128^3 and 256^3"},
             "learned": out}
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
