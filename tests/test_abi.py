@@ -42,3 +42,20 @@ def test_default_params_match_reference_defaults():
     assert (p.pre_smooth, p.post_smooth, p.final_smooth, p.bottom_smooth) == (2, 2, 8, 0)
     assert p.max_fmg_iter == 100000000 and p.bottom_max_iter == 200 and p.max_iter == 200
     assert p.bottom_tol_rel == 1e-4 and p.omega < 0
+    assert p.krylov == 0   # the FP32 cycles alone unless a caller asks for the GCR acceleration
+
+
+def test_params_struct_matches_header():
+    """The ctypes mirror of agb_solver_params lists the header's fields in the
+    header's order with the header's types (the struct crosses the ABI by
+    pointer)."""
+    import os
+    import re
+    from alamo_gb300 import _lib
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    src = open(os.path.join(root, "include", "agb.h")).read()
+    body = re.search(r"typedef struct \{([^}]*)\} agb_solver_params;", src).group(1)
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    fields = re.findall(r"\b(int|double)\s+(\w+)\s*;", body)
+    ctype = {"int": ctypes.c_int, "double": ctypes.c_double}
+    assert [(n, ctype[t]) for t, n in fields] == list(_lib.AgbSolverParams._fields_)
