@@ -147,6 +147,9 @@ public:
     void setPreSmooth(int v) { p_.pre_smooth = v; }
     void setPostSmooth(int v) { p_.post_smooth = v; }
     void setMixedPrecision(bool on) { p_.precision = on ? AGB_PREC_MIXED : AGB_PREC_F64; }
+    // mixed precision: flexible GCR over the FP32 cycle with k stored
+    // directions (0: the cycles alone, as MLMG iterates; no reference setter)
+    void setKrylov(int k) { p_.krylov = k; }
     const agb_solve_report& report() const { return last_; }
 
 protected:
