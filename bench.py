@@ -371,7 +371,7 @@ def run_rve(args, dist):
 def run_learned(args, dist):
     """Learned correction: train on 64^3 periodic RVEs, evaluate on unseen
     128^3 and 256^3 RVEs against plain FP64 multigrid, FP32-in-FP64
-    multigrid and V-cycle GCR (the ablation)."""
+    multigrid (alone and under GCR(8)) and V-cycle GCR (the ablation)."""
     import numpy as np
     import torch
     from alamo_gb300 import microstructure as M
@@ -396,6 +396,7 @@ def run_learned(args, dist):
         op.NewtonRHS(zero, zero, F0=F0n, out=rhs)
         row = {}
         for name, mk in (("mg_f64", lambda: Linear(op, precision=0)), ("mg_mixed", lambda: Linear(op, precision=1)),
+                         ("mg_mixed_gcr8", lambda: Linear(op, precision=1, krylov=8)),
                          ("gcr_v", lambda: LearnedSolver(op, None, restart=16)),
                          ("gcr_v_learned", lambda: LearnedSolver(op, net, restart=16))):
             s = mk()
