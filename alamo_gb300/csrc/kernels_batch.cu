@@ -401,7 +401,7 @@ __device__ __forceinline__ void cp_wait1() { asm volatile("cp.async.wait_group 1
 __device__ __forceinline__ void cp_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
 template <int SYM, int MODE>
-__global__ void __launch_bounds__(256) k_batch_pipe(const BProb* __restrict__ probs, const BTile* __restrict__ tiles,
+__global__ void __launch_bounds__(256, 3) k_batch_pipe(const BProb* __restrict__ probs, const BTile* __restrict__ tiles,
                                                     int ntiles, const int* __restrict__ active, int uniform,
                                                     const float* __restrict__ ddw, const float* __restrict__ x,
                                                     const float* __restrict__ b, const float* __restrict__ dinv,
@@ -472,7 +472,21 @@ __global__ void __launch_bounds__(256) k_batch_pipe(const BProb* __restrict__ pr
         issue(k0, true);
         issue(k0 + 1, true);
         issue(k0 + 2, true);
+        // b and 1/D of the own node, one plane ahead in registers
+        float bq[3] = {0, 0, 0}, dq[3] = {0, 0, 0};
+        auto fetch_bd = [&](int kk, float* bb, float* dd) {
+            if (!mine || kk >= k1) return;
+            const long long q0 = P.vo + L.idx(i, j, kk);
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                if (MODE != MODE_APPLY) bb[c] = __ldg(b + q0 + c * S);
+                if (MODE == MODE_JACOBI) dd[c] = __ldg(dinv + q0 + c * S);
+            }
+        };
+        fetch_bd(k0, bq, dq);
         for (int k = k0; k < k1; k++) {
+            float bn[3] = {0, 0, 0}, dn[3] = {0, 0, 0};
+            fetch_bd(k + 1, bn, dn);
             cp_wait1();   // every group but the newest (plane k+2) has landed
             __syncthreads();
             const int it = k - k0;
@@ -490,17 +504,22 @@ __global__ void __launch_bounds__(256) k_batch_pipe(const BProb* __restrict__ pr
                     const long long o = q0 + c * S;
                     if (MODE == MODE_APPLY) out[o] = f[c];
                     else if (MODE == MODE_RESID) {
-                        const float r = b[o] - f[c];
+                        const float r = bq[c] - f[c];
                         out[o] = r;
                         const float a = fabsf(r);
                         nrm = (a > nrm || a != a) ? a : nrm;
                     } else {
-                        out[o] = s.u[acc.u0][c][acc.h] + omega * ((b[o] - f[c]) * dinv[o]);
+                        out[o] = s.u[acc.u0][c][acc.h] + omega * ((bq[c] - f[c]) * dq[c]);
                     }
                 }
             }
 #pragma unroll
             for (int m = 0; m < NC; m++) acc.cm[m] = s.c[acc.c0][m][acc.h];
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                bq[c] = bn[c];
+                dq[c] = dn[c];
+            }
             __syncthreads();
             issue(k + 3, true);   // into the slots of u(k-1) and moduli(k)
         }
