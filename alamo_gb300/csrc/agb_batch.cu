@@ -67,6 +67,7 @@ struct BLevel {
     double *cor64 = nullptr, *res64 = nullptr, *rescor64 = nullptr, *tmp64 = nullptr;
     float *ddw32 = nullptr, *dinv32 = nullptr;
     float *cor32 = nullptr, *res32 = nullptr, *rescor32 = nullptr, *tmp32 = nullptr;
+    float* hold32 = nullptr;   // F-cycle's kept interpolated correction (GCR path only)
     double* work = nullptr;
 };
 
@@ -124,6 +125,7 @@ struct agb_batch_s {
     // per-problem GCR over the FP32 cycle (params.krylov > 0): directions,
     // their images, per-problem scalars, one graph per number of stored directions
     std::vector<float*> kZ, kW;
+    float* kr32 = nullptr;   // the GCR residual of each problem (the F-cycle overwrites res32 of level 0)
     double *kdots = nullptr, *kd2 = nullptr;
     std::vector<cudaGraphExec_t> gk;
     std::vector<long long> gk_k;
@@ -194,10 +196,14 @@ template <typename T> struct BEngine {
         }
     }
     // MLMG::mgVcycle(0, 0) for every problem, each with its own bottom level
-    void vcycle()
+    void vcycle() { vcycle_from(0, false); }
+    // MLMG::mgVcycle(0, top) for the problems that have level top; with
+    // skip_top_bottoms the problems whose bottom is level top are left alone
+    // (the F-cycle solved them already)
+    void vcycle_from(int top, bool skip_top_bottoms)
     {
         const int L = b->Lmax;
-        for (int l = 0; l < L; l++) {
+        for (int l = top; l < L; l++) {
             BLevel& v = b->lev[l];
             if (!v.t32_smooth.empty()) {
                 launch_batch_vec(b->st, BV_ZERO, b->grid, v.d_probs, v.c_t32_smooth, (int)v.t32_smooth.size(), act,
@@ -210,20 +216,59 @@ template <typename T> struct BEngine {
                 launch_batch_transfer<T>(b->st, 1, false, b->grid, v.d_probs, c.d_probs, c.c_t32_full,
                                          (int)c.t32_full.size(), act, A::rescor(v), A::res(c));
             }
-            if (!v.bottoms.empty())
-                launch_batch_bottom(b->st, b->sym, fp32, v.d_probs, v.d_bottoms, (int)v.bottoms.size(), act, b->bc,
-                                    false, fp32 ? (const void*)BArr<float>::ddw(v) : (const void*)v.ddw64, v.diag64,
-                                    A::cor(v), A::res(v), v.work, b->p.bottom_max_iter,
-                                    b->p.bottom_tol_rel, b->p.bottom_tol_abs, b->p.bottom_smooth, b->p.final_smooth,
-                                    b->omega);
+            if (!v.bottoms.empty() && !(skip_top_bottoms && l == top)) bottom(l);
         }
-        for (int l = L - 2; l >= 0; l--) {
+        for (int l = L - 2; l >= top; l--) {
             BLevel& v = b->lev[l];
             if (v.t32_smooth.empty()) continue;
             BLevel& c = b->lev[l + 1];
             launch_batch_transfer<T>(b->st, 0, false, b->grid, v.d_probs, c.d_probs, v.c_t32_smooth,
                                      (int)v.t32_smooth.size(), act, A::cor(c), A::cor(v));
             smooth(l, A::cor(v), A::res(v), b->p.post_smooth);
+        }
+    }
+    void bottom(int l)
+    {
+        BLevel& v = b->lev[l];
+        launch_batch_bottom(b->st, b->sym, fp32, v.d_probs, v.d_bottoms, (int)v.bottoms.size(), act, b->bc, false,
+                            fp32 ? (const void*)BArr<float>::ddw(v) : (const void*)v.ddw64, v.diag64, A::cor(v),
+                            A::res(v), v.work, b->p.bottom_max_iter, b->p.bottom_tol_rel, b->p.bottom_tol_abs,
+                            b->p.bottom_smooth, b->p.final_smooth, b->omega);
+    }
+    // MLMG::mgFcycle for every problem (FP32; needs hold32 on every level):
+    // the residual restricted to each problem's bottom and solved there, then
+    // on the way up each level takes the prolonged correction, a V-cycle from
+    // that level on the residual of it, and the sum.  The roles of res/rescor
+    // and cor/hold are swapped around the V-cycle instead of copying, and
+    // swapped back (the captured graph replays from the same roles).
+    void fcycle()
+    {
+        const int L = b->Lmax;
+        for (int l = 0; l + 1 < L; l++) {
+            BLevel& v = b->lev[l];
+            if (v.t32_smooth.empty()) continue;
+            BLevel& c = b->lev[l + 1];
+            launch_batch_transfer<T>(b->st, 1, false, b->grid, v.d_probs, c.d_probs, c.c_t32_full,
+                                     (int)c.t32_full.size(), act, A::res(v), A::res(c));
+        }
+        for (int l = 0; l < L; l++)
+            if (!b->lev[l].bottoms.empty()) bottom(l);
+        for (int l = L - 2; l >= 0; l--) {
+            BLevel& v = b->lev[l];
+            if (v.t32_smooth.empty()) continue;
+            BLevel& c = b->lev[l + 1];
+            launch_batch_transfer<T>(b->st, 0, true, b->grid, v.d_probs, c.d_probs, v.c_t32_smooth,
+                                     (int)v.t32_smooth.size(), act, A::cor(c), A::cor(v));
+            launch_batch_stencil<T>(b->st, b->sym, MODE_RESID, v.shape, b->grid, v.d_probs, v.c_tS_smooth,
+                                    (int)v.tS_smooth.size(), act, b->bc, false, A::ddw(v), A::cor(v), A::res(v),
+                                    nullptr, A::rescor(v), (T)0, nullptr);
+            std::swap(v.res32, v.rescor32);
+            std::swap(v.cor32, v.hold32);
+            vcycle_from(l, true);
+            launch_batch_vec(b->st, BV_AXPY, b->grid, v.d_probs, v.c_t32_smooth, (int)v.t32_smooth.size(), act,
+                             v.hold32, v.cor32, 1.0, nullptr, 1);
+            std::swap(v.res32, v.rescor32);
+            std::swap(v.cor32, v.hold32);
         }
     }
 };
@@ -527,7 +572,10 @@ void gcr_iter_body(agb_batch b, int k)
     const int* act = b->d_iactive;
     const int np = b->np;
     BEngine<float> E{b, act};
-    E.vcycle();
+    launch_batch_vec(b->st, BV_COPY, b->grid, v0.d_probs, v0.c_t32_full, (int)v0.t32_full.size(), act, v0.res32,
+                     b->kr32, 0.0, nullptr, 1);
+    if (b->p.max_fmg_iter > 0) E.fcycle();
+    else E.vcycle();
     float* z = b->kZ[k];
     float* w = b->kW[k];
     launch_batch_vec(b->st, BV_COPY, b->grid, v0.d_probs, v0.c_t32_full, (int)v0.t32_full.size(), act, z, v0.cor32,
@@ -553,18 +601,21 @@ void gcr_iter_body(agb_batch b, int k)
     }
     GcrVecs P;
     P.v[0] = w;
-    P.v[1] = v0.res32;
+    P.v[1] = b->kr32;
     launch_batch_multidot(b->st, b->grid, v0.d_probs, v0.c_t32_full, (int)v0.t32_full.size(), act, 2, w, P,
                           v0.dinv32, b->kd2, 2);
     cudaMemsetAsync(b->d_norms, 0, sizeof(double) * np, b->st);
     launch_batch_gcr_step(b->st, b->grid, v0.d_probs, v0.c_t32_full, (int)v0.t32_full.size(), act, b->kd2, w, z,
-                          b->sol32, v0.res32, b->d_norms);
+                          b->sol32, b->kr32, b->d_norms);
     cudaMemcpyAsync(b->h_norms, b->d_norms, sizeof(double) * np, cudaMemcpyDeviceToHost, b->st);
 }
 
 agb_status gcr_setup(agb_batch b, int m)
 {
     BLevel& v0 = b->lev[0];
+    if (b->p.max_fmg_iter > 0)
+        for (auto& v : b->lev)
+            if (!v.hold32 && v.nvec > 0) BTRY(b->alloc(&v.hold32, v.nvec));
     while ((int)b->kZ.size() < m) {
         float *z = nullptr, *w = nullptr;
         BTRY(b->alloc(&z, v0.nvec));
@@ -575,6 +626,7 @@ agb_status gcr_setup(agb_batch b, int m)
     if (!b->kdots) {
         BTRY(b->alloc(&b->kdots, (size_t)b->np * GCR_MAX));
         BTRY(b->alloc(&b->kd2, (size_t)b->np * 2));
+        BTRY(b->alloc(&b->kr32, v0.nvec));
     }
     b->gk.resize(m, nullptr);
     b->gk_k.resize(m, 0);
@@ -780,7 +832,7 @@ agb_status agb_batch_solve(agb_batch b, double tol_rel, double tol_abs, agb_solv
             launch_batch_vec(b->st, BV_SCALE_TO32, b->grid, v0.d_probs, v0.d_t32_full, (int)v0.t32_full.size(),
                              b->d_active, b->rhs32, v0.res64, 0.0, b->scale, 1);
             launch_batch_vec(b->st, BV_COPY, b->grid, v0.d_probs, v0.d_t32_full, (int)v0.t32_full.size(), b->d_active,
-                             v0.res32, b->rhs32, 0.0, nullptr, 1);
+                             m > 0 ? b->kr32 : v0.res32, b->rhs32, 0.0, nullptr, 1);
             launch_batch_vec(b->st, BV_ZERO, b->grid, v0.d_probs, v0.d_t32_full, (int)v0.t32_full.size(), b->d_active,
                              b->sol32, nullptr, 0.0, nullptr, 1);
             std::vector<int> slow(np, 0);
