@@ -1332,9 +1332,11 @@ agb_status agb_learned_solve(agb_solver s, agb_learned net, double* sol, const d
     const bool sing = L0.singular();
     if (sing) launch_remove_mean<double>(st, L0, s->b64, op->d_slots + 8);
     const long long nall = (long long)n3;
+    // inner product weighted by 1/diag^2 (rows scaled to a unit diagonal, as in
+    // the mixed solve's inner GCR)
     auto dot = [&](const double* a, const double* b, double* outv) -> agb_status {
         CK(cudaMemsetAsync(s->gdot, 0, sizeof(double), st));
-        launch_dot(st, nall, a, b, s->gdot);
+        launch_dot(st, nall, a, b, s->gdot, v0.dinv64);
         CK(cudaMemcpyAsync(op->h_slots + 12, s->gdot, sizeof(double), cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
         *outv = op->h_slots[12];

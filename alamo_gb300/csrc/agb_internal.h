@@ -201,7 +201,9 @@ void launch_gcr_orth(cudaStream_t st, long long n, int k, const double* beta, co
 void launch_gcr_step(cudaStream_t st, long long n, const double* dots, float* w, float* z, float* c, float* r,
                      void* slot);
 // *out += sum x[e] y[e] over n elements (padding entries are zero in every vector)
-void launch_dot(cudaStream_t st, long long n, const double* x, const double* y, double* out);
+// sum x y, or sum x y w^2 when w is given
+void launch_dot(cudaStream_t st, long long n, const double* x, const double* y, double* out,
+                const double* w = nullptr);
 // learned correction network (learned.cu)
 bool learned_box_ok(const LevelDesc& L);
 agb_status learned_apply(agb_learned net, cudaStream_t st, const LevelDesc& L, const double* r, const double* ddw64,

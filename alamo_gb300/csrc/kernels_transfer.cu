@@ -424,18 +424,20 @@ void launch_remove_mean(cudaStream_t st, const LevelDesc& L, T* x, double* sums3
     count_launch();
 }
 
-__global__ void k_dot(long long n, const double* __restrict__ x, const double* __restrict__ y, double* __restrict__ out)
+// sum x y (w == nullptr) or sum x y w^2
+__global__ void k_dot(long long n, const double* __restrict__ x, const double* __restrict__ y,
+                      const double* __restrict__ w, double* __restrict__ out)
 {
     double s = 0;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
-        s += x[e] * y[e];
+        s += w ? x[e] * y[e] * (w[e] * w[e]) : x[e] * y[e];
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     if ((threadIdx.x & 31) == 0) atomicAdd(out, s);
 }
 
-void launch_dot(cudaStream_t st, long long n, const double* x, const double* y, double* out)
+void launch_dot(cudaStream_t st, long long n, const double* x, const double* y, double* out, const double* w)
 {
-    k_dot<<<blocks_1d(n), 256, 0, st>>>(n, x, y, out);
+    k_dot<<<blocks_1d(n), 256, 0, st>>>(n, x, y, w, out);
     count_launch();
 }
 
