@@ -108,6 +108,40 @@ def sphere_inclusion(n=64, radius=0.25, lam_m=1.0, mu_m=1.0, lam_i=10.0, mu_i=10
     return ddw.reshape(-1), F0.reshape(-1)
 
 
+def ellipse_eta(n, prob_lo, prob_hi, a, x0=(0.0, 0.0, 0.0), eps=0.1):
+    """IC::Ellipse (IC/Ellipse.H:58-59) at the nodes of an n^3-cell box:
+    eta = 1/2 - 1/2 erf(((x-x0)^T A (x-x0) - 1) / eps / |A (x-x0)|), A =
+    diag(1/a^2).  (n+1)^3 values, i fastest; at x = x0 (0/0) eta = 1."""
+    from math import erf
+    ax = [prob_lo[d] + (prob_hi[d] - prob_lo[d]) * np.arange(n + 1) / n for d in range(3)]
+    Z, Y, X = np.meshgrid(ax[2], ax[1], ax[0], indexing="ij")
+    d = [X - x0[0], Y - x0[1], Z - x0[2]]
+    A = [1.0 / (a[k] * a[k]) for k in range(3)]
+    q = sum(A[k] * d[k] * d[k] for k in range(3))
+    norm = np.sqrt(sum((A[k] * d[k]) ** 2 for k in range(3)))
+    with np.errstate(divide="ignore", invalid="ignore"):
+        arg = (q - 1.0) / eps / norm
+    arg = np.where(norm > 0, arg, -np.inf)
+    verf = np.vectorize(lambda v: erf(v) if np.isfinite(v) else np.sign(v))
+    return (0.5 - 0.5 * verf(arg)).reshape(-1)
+
+
+def eshelby_problem(n, gd):
+    """The reference's tests/Eshelby configuration on one uniform level of n^3
+    cells (gd: tests/golden/eshelby_kat.json): affine isotropic moduli from E,
+    nu everywhere and the eigenstrain F0_inside weighted by the ellipse eta
+    (Integrator/Mechanics.H:249-253 mixing, both models share E and nu).
+    Returns (ddw AoS (lambda, mu) per node, F0 AoS 9 per node)."""
+    E, nu = gd["E"], gd["nu"]
+    lam = E * nu / (1 + nu) / (1 - 2 * nu)
+    mu = E / 2 / (1 + nu)
+    el = gd["ellipse"]
+    eta = ellipse_eta(n, gd["prob_lo"], gd["prob_hi"], el["a"], el["x0"], el["eps"])
+    ddw = np.tile([lam, mu], eta.size)
+    F0 = (eta[:, None] * np.asarray(gd["F0_inside"], float)[None, :]).reshape(-1)
+    return ddw, F0
+
+
 def voronoi_seeds(ngrains=64, seed=20260, C11=1.68, C12=1.21, C44=0.75):
     rng = SplitMix64(seed)
     pts = np.array([[rng.uniform() for _ in range(3)] for _ in range(ngrains)])

@@ -1,5 +1,5 @@
 """Extract the reference's known-answer data for the elastic path into
-tests/golden/solid_kat.json.
+tests/golden/solid_kat.json and tests/golden/eshelby_kat.json.
 
 Run here (where the reference tree is mounted); the JSON travels with the
 repository.  Sources (paths relative to the alamo tree):
@@ -9,6 +9,12 @@ repository.  Sources (paths relative to the alamo tree):
   tests/Solid/reference/linear-cubic.dat, affine-cubic.dat   trac_xhi_x vs time
   tests/UniaxialTension/input, tests/UniaxialTension/test    analytic u_x, sigma_xx,
                                                       tolerance 1e-8
+  tests/Eshelby/input, tests/Eshelby/test             ellipsoidal inclusion (affine.isotropic,
+                                                      eigenstrain 1e-3 I inside), box [-8,8]^3,
+                                                      zero displacement on the faces
+  tests/Eshelby/reference/Eshelby_displacement.csv, Eshelby_sigma_normal.csv
+                                                      analytic profiles along the ray
+                                                      x = y = 0.25, z in [-2, 2]; tolerance 0.1
 """
 import json
 import os
@@ -16,6 +22,14 @@ import sys
 
 REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "solid_kat.json")
+OUT_ESHELBY = os.path.join(os.path.dirname(os.path.abspath(__file__)), "eshelby_kat.json")
+
+
+def load_csv(path):
+    with open(path) as f:
+        head = f.readline().strip().split(",")
+        rows = [list(map(float, line.split(","))) for line in f if line.strip()]
+    return {h: [r[i] for r in rows] for i, h in enumerate(head)}
 
 
 def load_dat(path):
@@ -61,6 +75,23 @@ def main():
     with open(OUT, "w") as f:
         json.dump(out, f, indent=1)
     print("wrote", OUT)
+    esh = os.path.join(REF, "tests", "Eshelby")
+    eshelby = {
+        "source": "alamo tests/Eshelby (input, test, reference/*.csv)",
+        "prob_lo": [-8.0, -8.0, -8.0], "prob_hi": [8.0, 8.0, 8.0],
+        "E": 210.0, "nu": 0.3,
+        "F0_inside": [0.001, 0, 0, 0, 0.001, 0, 0, 0, 0.001],
+        "ellipse": {"a": [1.0, 0.75, 0.5], "x0": [0.0, 0.0, 0.0], "eps": 0.1},
+        "ray": {"x": 0.25, "y": 0.25, "z": [-2.0, 2.0]},
+        "tolerance": 0.1,
+        # the reference script scales the tables: displacement / 10000, stress * 210 / 1000
+        "disp_scale": 1.0 / 10000.0, "sigma_scale": 210.0 / 1000.0,
+        "displacement": load_csv(os.path.join(esh, "reference", "Eshelby_displacement.csv")),
+        "sigma_normal": load_csv(os.path.join(esh, "reference", "Eshelby_sigma_normal.csv")),
+    }
+    with open(OUT_ESHELBY, "w") as f:
+        json.dump(eshelby, f, indent=0)
+    print("wrote", OUT_ESHELBY)
 
 
 if __name__ == "__main__":

@@ -90,3 +90,28 @@ def uniaxial_tension_bc():
 
 def rel_err(a, b):
     return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def eshelby_errors(gd, z, u, sig):
+    """The metrics of the reference's tests/Eshelby/test along its ray: for
+    the displacement the relative L2 error sqrt(int (ref - u)^2 / int ref^2),
+    for the normal stresses the relative 1-norm error int |ref - sig| /
+    int |ref|, the reference tables scaled as the script scales them and
+    interpolated at the sample points z (trapezoidal integrals)."""
+    import numpy as np
+
+    def integrate(x, y):
+        return float(np.sum(0.5 * (y[1:] + y[:-1]) * np.diff(x)))
+
+    dref = gd["displacement"]
+    sref = gd["sigma_normal"]
+    xd = np.asarray(dref["x"])
+    xs = np.asarray(sref["x"])
+    out = {}
+    for c, key in enumerate(("disp1", "disp2", "disp3")):
+        r = np.asarray(dref[key]) * gd["disp_scale"]
+        out["u%d" % (c + 1)] = np.sqrt(integrate(z, (np.interp(z, xd, r) - u[c]) ** 2) / integrate(xd, r ** 2))
+    for c, key in enumerate(("sigma11", "sigma22", "sigma33")):
+        r = np.asarray(sref[key]) * gd["sigma_scale"]
+        out["sig%d%d" % (c + 1, c + 1)] = integrate(z, np.abs(np.interp(z, xs, r) - sig[c])) / integrate(xs, np.abs(r))
+    return out
