@@ -12,7 +12,9 @@ from .elastic import _ptr, default_params
 class Batch:
     def __init__(self, sizes, dx=None, sym="isotropic", periodic=(1, 1, 1), **params):
         """sizes: list of (nx, ny, nz) cells per problem; dx: list of cell sizes
-        (default 1/n: unit cubes)."""
+        (default 1/n: unit cubes); params: agb_solver_params fields, e.g.
+        precision=1 (FP32 cycles in FP64 refinement) and krylov=8 (each
+        problem's GCR over the batched FP32 cycle)."""
         self.sizes = [tuple(int(v) for v in s) for s in sizes]
         self.np = len(self.sizes)
         if dx is None:

@@ -317,7 +317,10 @@ def default_params(**kw):
 
 
 class Linear:
-    """Solver::Nonlocal::Linear (Linear.H:18-392) over the GPU MLMG driver."""
+    """Solver::Nonlocal::Linear (Linear.H:18-392) over the GPU MLMG driver.
+    params: agb_solver_params fields (Linear::Parse's keys, Linear.H:296-382),
+    plus precision=1 (FP32 cycles in FP64 refinement) and krylov=k (flexible
+    GCR over the FP32 cycle with k stored directions; no reference key)."""
 
     def __init__(self, op=None, **params):
         self.params = default_params(**params)
