@@ -79,6 +79,23 @@ long long& launch_counter()
     return n;
 }
 void set_error(const char* msg) { g_err = msg ? msg : ""; }
+int sm_count()
+{
+    static int cache[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        cudaGetLastError();
+        return 1;
+    }
+    int v = __atomic_load_n(&cache[dev], __ATOMIC_RELAXED);
+    if (v > 0) return v;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v < 1) {
+        cudaGetLastError();
+        return 1;
+    }
+    __atomic_store_n(&cache[dev], v, __ATOMIC_RELAXED);
+    return v;
+}
 }  // namespace agb
 
 struct agb_op_s {

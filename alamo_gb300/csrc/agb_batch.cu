@@ -131,7 +131,7 @@ struct agb_batch_s {
     std::vector<long long> gk_k;
     long long compact_tiles = -1;   // level-0 tiles in the compacted lists (-1: not built)
     std::vector<int> compact_mask;
-    int grid = 152 * 4;
+    int grid = 0;   // persistent grid: 4 CTAs per SM, set at creation
     bool model_set = false, prepared = false, tuned = false, f0_set = false;
     std::vector<void*> allocs;
 
@@ -673,10 +673,7 @@ agb_status agb_batch_create(int nprob, const int* n_cells, const double* dx, con
     cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking);
     cudaEventCreate(&b->e0);
     cudaEventCreate(&b->e1);
-    int dev = 0, sms = 152;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    b->grid = sms * 4;
+    b->grid = sm_count() * 4;
     const agb_status s = build_levels(b);
     if (s != AGB_OK) {
         agb_batch_destroy(b);

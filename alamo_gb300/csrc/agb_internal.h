@@ -76,6 +76,9 @@ inline LevelDesc make_level(const int n[3], const int per[3], const double dx[3]
 // this process; the benchmark reports kernels per solve from it.
 long long& launch_counter();
 inline void count_launch() { ++launch_counter(); }
+// Streaming multiprocessors of the current device (queried once per device;
+// 1 if the query fails, which only shrinks grid-stride grids).
+int sm_count();
 // Sets the thread-local message agb_last_error() returns.
 void set_error(const char* msg);
 

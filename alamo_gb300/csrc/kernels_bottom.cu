@@ -636,8 +636,9 @@ template void launch_bottom<float>(cudaStream_t, int, const LevelDesc&, const BC
 //
 // Some callers may not allocate device memory at the moment they need a
 // bottom solve: a host framework that owns every device byte through its own
-// arena and forbids cudaMalloc inside its solver hooks, or code that runs
-// while a stream is being captured into a CUDA graph.  For them the BiCGStab
+// arena and forbids cudaMalloc inside its solver hooks, or a time-stepping
+// code that must not stall on cudaMalloc's implicit synchronisation in the
+// middle of a step.  For them the BiCGStab
 // work vectors live in a file-scope device array instead of a buffer of an
 // operator handle.  The array is sized for boxes of at most
 // AGB_NOALLOC_MAX_NODES nodes (a 16^3-cell box); every GPU that loads this
@@ -658,7 +659,11 @@ double* g_scratch_addr[kMaxDevices] = {nullptr};
 
 // Device address of g_bottom_scratch on the current device.  The name
 // g_bottom_scratch is only a host-side stand-in: a kernel must be given the
-// address that cudaGetSymbolAddress returns for the device it runs on.
+// address that cudaGetSymbolAddress returns for the device it runs on.  The
+// address is cached per device for the life of the process, which assumes
+// one CUDA context per device: after cudaDeviceReset the cached address is
+// stale, so a caller that resets a device must not call this entry point
+// again in that process.
 agb_status scratch_for_current_device(double** out)
 {
     int dev = 0;
@@ -714,6 +719,10 @@ extern "C" agb_status agb_bottom_solve_noalloc(const int n_cells[3], const doubl
         set_error("box too large for the allocation-free bottom solve: more than AGB_NOALLOC_MAX_NODES nodes");
         return AGB_BADARG;
     }
+    if (cor == res) {
+        set_error("res and cor must be distinct, non-overlapping arrays");
+        return AGB_BADARG;
+    }
     if (max_iter < 0 || bottom_smooth < 0 || final_smooth < 0 || !(omega > 0 && omega < 2)) {
         set_error("bad iteration count, smoothing count or omega");
         return AGB_BADARG;
@@ -723,6 +732,12 @@ extern "C" agb_status agb_bottom_solve_noalloc(const int n_cells[3], const doubl
         for (int c = 0; c < 3; c++) {
             if (bc->type[f][c] < AGB_BC_DISP || bc->type[f][c] > AGB_BC_NONE) {
                 set_error("bad BC type");
+                return AGB_BADARG;
+            }
+            // The box has no periodic direction: a periodic row would be an
+            // empty row (zero diagonal) of the scaled system.
+            if (bc->type[f][c] == AGB_BC_PERIODIC) {
+                set_error("the allocation-free bottom solve takes no periodic BC type");
                 return AGB_BADARG;
             }
             t.type[f][c] = (int8_t)bc->type[f][c];
@@ -742,6 +757,10 @@ extern "C" agb_status agb_bottom_solve_noalloc(const int n_cells[3], const doubl
     double* work = nullptr;
     const agb_status s = scratch_for_current_device(&work);
     if (s != AGB_OK) return s;
+    // An error pending from earlier, unrelated work is not this call's: clear
+    // it, so that the check after the launch sees only the launch's own
+    // error (a broken context makes the launch itself fail).
+    if (cudaPeekAtLastError() != cudaSuccess) cudaGetLastError();
     // Every scratch element the kernel reads is written earlier in the same
     // launch, so the contents left by a previous call need no clearing.
     launch_bottom<double>((cudaStream_t)stream, sym, L, t, uniform != 0, ddw, diag, cor, res, work, max_iter, tol_rel,

@@ -323,7 +323,8 @@ __global__ void k_adam(long long count, float* __restrict__ w, const float* __re
 int conv_blocks(long long n)
 {
     const long long b = (n + 255) / 256;
-    return (int)(b < 152 * 8 ? (b < 1 ? 1 : b) : 152 * 8);
+    const long long cap = 8LL * sm_count();
+    return (int)(b < cap ? (b < 1 ? 1 : b) : cap);
 }
 
 bool conv_box_ok(const int n[3]) { return n[0] % CX == 0 && n[1] % CY == 0 && n[2] % CZ == 0 && n[0] > 0; }
@@ -458,7 +459,7 @@ extern "C" agb_status agb_conv3_wgrad(const int n[3], int cinp, int coutp, const
     const int tg = std::min(27, std::max(1, 8 * WG_MAX_OWN / (MT * NTc)));
     const int ngroups = (27 + tg - 1) / tg;
     const int ntile = (n[0] / CX) * (n[1] / CY) * (n[2] / CZ);
-    const int gx = std::max(1, std::min(ntile, 152 * 2 / ngroups + 1));
+    const int gx = std::max(1, std::min(ntile, sm_count() * 2 / ngroups + 1));
     cudaStream_t st = (cudaStream_t)stream;
     const size_t sm = wgrad_smem(cinp, coutp);
     dim3 grid(gx, ngroups);
@@ -471,7 +472,7 @@ extern "C" agb_status agb_conv3_wgrad(const int n[3], int cinp, int coutp, const
     count_launch();
     if (db) {
         const long long nvox = (long long)n[0] * n[1] * n[2];
-        k_bias_grad<<<dim3(152, coutp), 256, 0, st>>>(nvox, coutp, (const __nv_bfloat16*)dy, db);
+        k_bias_grad<<<dim3(sm_count(), coutp), 256, 0, st>>>(nvox, coutp, (const __nv_bfloat16*)dy, db);
         count_launch();
     }
     const cudaError_t e = cudaGetLastError();

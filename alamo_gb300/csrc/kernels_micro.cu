@@ -125,7 +125,8 @@ __global__ void k_gen_sphere(Box b, double R, double lm, double mm, double li, d
 int gen_blocks(long long n)
 {
     const long long b = (n + 255) / 256;
-    return (int)(b < 152 * 8 ? (b < 1 ? 1 : b) : 152 * 8);
+    const long long cap = 8LL * sm_count();
+    return (int)(b < cap ? (b < 1 ? 1 : b) : cap);
 }
 
 // Device scratch for host-side outputs and the parameter tables.

@@ -343,7 +343,7 @@ static bool launch_tma_sm(cudaStream_t st, const LevelDesc& L, bool uniform, con
     const Geo<float> g = make_geo<float>(L);
     dim3 blk(TT_X, TT_Y, 1);
     // k-chunk: the longest (least halo re-read) that still gives at least
-    // three waves of 2 CTAs on each of the 152 SMs, and no shorter than 4
+    // three waves of 2 CTAs on each SM, and no shorter than 4
     // planes (AGB_TMA_KZ_MIN)
     const int cxy = ((L.n[0] - 1 + TT_X - 1) / TT_X) * ((L.n[1] - 1 + TT_Y - 1) / TT_Y);
     static const int kz_min = [] {
@@ -352,7 +352,7 @@ static bool launch_tma_sm(cudaStream_t st, const LevelDesc& L, bool uniform, con
         return v >= 1 && v <= TT_Z ? v : 4;
     }();
     int kz = TT_Z;
-    while (kz > kz_min && (long long)cxy * ((L.n[2] - 1 + kz - 1) / kz) < 3 * 2 * 152) kz /= 2;
+    while (kz > kz_min && (long long)cxy * ((L.n[2] - 1 + kz - 1) / kz) < 3LL * 2 * sm_count()) kz /= 2;
     dim3 grd((L.n[0] - 1 + TT_X - 1) / TT_X, (L.n[1] - 1 + TT_Y - 1) / TT_Y, (L.n[2] - 1 + kz - 1) / kz);
     k_stencil_tma<SYM, MODE><<<grd, blk, TmaLayout<SYM>::SMEM, st>>>(L, g, uniform ? 1 : 0, mx, mc, ddw, b, dinv,
                                                                      out, omega, norm_slot, err, kz);

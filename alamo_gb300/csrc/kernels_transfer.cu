@@ -331,7 +331,8 @@ __global__ void k_mean3(LevelDesc L, T* __restrict__ x, double* __restrict__ sum
 static inline int blocks_1d(long long n)
 {
     long long b = (n + 255) / 256;
-    return (int)(b < 152 * 16 ? (b < 1 ? 1 : b) : 152 * 16);
+    const long long cap = 16LL * sm_count();
+    return (int)(b < cap ? (b < 1 ? 1 : b) : cap);
 }
 
 template <typename T>

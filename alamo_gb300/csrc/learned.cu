@@ -95,7 +95,8 @@ __global__ void k_pack_ref(int n0, int n1, int n2, const double* __restrict__ r,
 int lblocks(long long n)
 {
     const long long b = (n + 255) / 256;
-    return (int)(b < 152 * 8 ? (b < 1 ? 1 : b) : 152 * 8);
+    const long long cap = 8LL * sm_count();
+    return (int)(b < cap ? (b < 1 ? 1 : b) : cap);
 }
 
 }  // namespace

@@ -122,7 +122,10 @@ def ellipse_eta(n, prob_lo, prob_hi, a, x0=(0.0, 0.0, 0.0), eps=0.1):
     with np.errstate(divide="ignore", invalid="ignore"):
         arg = (q - 1.0) / eps / norm
     arg = np.where(norm > 0, arg, -np.inf)
-    verf = np.vectorize(lambda v: erf(v) if np.isfinite(v) else np.sign(v))
+    try:
+        from scipy.special import erf as verf   # vectorised; erf(+-inf) = +-1
+    except ImportError:
+        verf = np.vectorize(lambda v: erf(v) if np.isfinite(v) else np.sign(v))
     return (0.5 - 0.5 * verf(arg)).reshape(-1)
 
 

@@ -12,11 +12,13 @@ plain FP64 multigrid solve of the same system is timed once beside it.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-`--impl reference` times the CPU restatement of the reference algorithm
-(oracle/, OpenMP on every host core) on a bounded sample of the same workload.
+`--impl reference` times one complete solve of the same system by the CPU
+restatement of the reference algorithm (oracle/, FP64 MLMG F-cycles, OpenMP on
+every host core), split over the timed steps.
 """
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -24,6 +26,8 @@ import sys
 import tempfile
 import threading
 import time
+
+import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
@@ -225,11 +229,15 @@ def run_ours(args, dist):
     step_ms = dist.max(statistics.mean(dev_ms))
     kernels = int(sum(r.kernels for r in reps))
     last = reps[-1]
+    if any(r.status != 0 for r in reps):
+        raise RuntimeError("a timed solve did not converge: statuses %s" % [r.status for r in reps])
     res = {
         "step_ms": step_ms, "wall_ms": wall * 1000 / args.steps, "kernels": kernels, "clocks": clk,
         "mixed": {"cycles": last.iterations, "refinements": last.refinements, "res0": last.res0,
-                  "res_final": last.res_final, "rhs_norm": last.rhs_norm, "nlevels": last.nlevels},
+                  "res_final": last.res_final, "rhs_norm": last.rhs_norm, "nlevels": last.nlevels,
+                  "res_rel_final": last.res_final / max(last.rhs_norm, last.res0)},
     }
+    x_mixed = sol_d.clone()
 
     # roofline of the dominant kernel: the FP32 damped-Jacobi sweep on the finest level
     ms_j32 = op.time_sweep(0, "f32", 2, 20)
@@ -245,8 +253,14 @@ def run_ours(args, dist):
         plain.solve(sol_d, rhs_d, 1e-8, 0.0)
         pr = plain.report
         res["plain"] = {"ms": pr.solve_ms, "iterations": pr.iterations, "res_final": pr.res_final,
-                        "status": pr.status}
+                        "status": pr.status, "res_rel_final": pr.res_final / max(pr.rhs_norm, pr.res0)}
+        # the timed mixed solution against the plain FP64 solution of the same
+        # system (max-norm relative displacement difference)
+        res["err_vs_fp64"] = float((x_mixed - sol_d).abs().max().item() / sol_d.abs().max().item())
         plain.Clear()
+    res["x_mixed"] = x_mixed.cpu().numpy()
+    res["rhs"] = rhs_h
+    del x_mixed
 
     # end to end through the reference-facing calls with host buffers:
     # SetModel(host Matrix4 field) + Newton step (host u, host b) -> host u
@@ -288,23 +302,42 @@ def run_ours(args, dist):
     return res, ddw_h, bc
 
 
-def cpu_sample(n, ddw_h, bc, iterations):
-    """The oracle on every host core: prepareForSolve + one MLMG F-cycle
-    iteration at the full size, scaled to a full solve by `iterations`."""
-    import numpy as np
+def oracle_grid(n, bc):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
-    g = O.make_grid([n] * 3, sym=O.MAJORMINOR, bc_type=bc.type, bc_val=bc.val)
-    N = O.nodes(g)
-    b = O.bc_init(g, np.zeros(3 * N))
-    rhs = O.newton_rhs(g, ddw_h, None, np.zeros(3 * N), b)
-    _, rep = O.solve(g, ddw_h, rhs, tol_rel=1e-8, tol_abs=0.0, params=O.default_params(max_iter=1))
+    return O, O.make_grid([n] * 3, sym=O.MAJORMINOR, bc_type=bc.type, bc_val=bc.val)
+
+
+def cpu_sample(n, ddw_h, bc, rhs, iterations, k=2):
+    """Bounded sample of the CPU leg: the oracle on every host core runs
+    prepareForSolve and `k` MLMG F-cycle iterations of the same 257^3 solve
+    (about 10 s); the full-solve time is that setup plus `iterations` (the
+    FP64 F-cycle count the GPU plain solve of the same system took in this
+    run; the oracle's count equals it within one, as the parity tests check)
+    times the measured time per iteration."""
+    O, g = oracle_grid(n, bc)
+    t0 = time.perf_counter()
+    sess = O.Session(g, ddw_h, rhs, tol_rel=1e-8, tol_abs=0.0)
+    t1 = time.perf_counter()
+    sess.iterate(k)
+    t2 = time.perf_counter()
+    _, rep = sess.finish()
     cores = O.lib().orc_num_threads()
-    value = rep.t_setup + iterations * rep.t_iter
+    per_iter = (t2 - t1) / max(rep.iterations, 1)
+    value = (t1 - t0) + iterations * per_iter
     return {"value": value, "unit": "s", "cores": cores, "kind": "port",
-            "sample": "oracle/ CPU restatement, OpenMP %d threads: prepareForSolve + 1 F-cycle iteration at "
-                      "257^3 measured (%.2f s + %.2f s), scaled by the %d iterations the same FP64 algorithm "
-                      "needs" % (cores, rep.t_setup, rep.t_iter, iterations)}
+            "sample": "oracle/ CPU restatement, OpenMP %d threads, same %d^3-node system: prepareForSolve (%.2f s) + "
+                      "%d F-cycle iterations (%.2f s each) measured, scaled to the %d iterations the plain FP64 "
+                      "solve took on the GPU in this run" % (cores, n + 1, t1 - t0, rep.iterations, per_iter,
+                                                             iterations)}
+
+
+def oracle_check(n, ddw_h, bc, x, rhs):
+    """The oracle's FP64 residual of the GPU solution (max norm, relative to
+    ||rhs||): the checker's verdict on the timed result."""
+    O, g = oracle_grid(n, bc)
+    r = O.residual(g, ddw_h, x, rhs)
+    return float(np.abs(r).max() / np.abs(rhs).max())
 
 
 def run_rve(args, dist):
@@ -457,9 +490,14 @@ def main():
     if "plain" in res:
         extra["plain_fp64_s"] = res["plain"]["ms"] / 1000.0
         extra["plain_fp64_iterations"] = res["plain"]["iterations"]
+        extra["plain_fp64_res_rel_final"] = res["plain"]["res_rel_final"]
         extra["speedup_vs_plain_fp64"] = round(res["plain"]["ms"] / res["step_ms"], 2)
+        extra["err_vs_fp64"] = res["err_vs_fp64"]
+    extra["res_rel_final"] = res["mixed"]["res_rel_final"]
+    # a replica solves one system per GPU: the value is the time of one solve
+    # (max over ranks), not divided by the number of replicas
     line = {
-        "metric": METRIC, "value": res["step_ms"] / 1000.0 / dist.world, "unit": "s", "n_gpus": dist.world,
+        "metric": METRIC, "value": res["step_ms"] / 1000.0, "unit": "s", "n_gpus": dist.world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["step_ms"], "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic (seeded Voronoi polycrystal)",
@@ -477,9 +515,10 @@ def main():
         line["e2e"] = res["e2e"]
     line.update(extra)
     if dist.rank == 0 and not args.no_cpu:
+        line["res_rel_oracle"] = oracle_check(args.n, ddw_h, bc, res["x_mixed"], res["rhs"])
         iters = res.get("plain", {}).get("iterations") or 0
         if iters:
-            line["cpu_baseline"] = cpu_sample(args.n, ddw_h, bc, iters)
+            line["cpu_baseline"] = cpu_sample(args.n, ddw_h, bc, res["rhs"], iters)
     dist.barrier()
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
@@ -489,55 +528,60 @@ def main():
 # ---------------------------------------------------------------------------
 # reference arm: the CPU restatement of the reference algorithm
 # ---------------------------------------------------------------------------
-ITERATIONS_FILE = os.path.join(ROOT, "profiles", "c2_iterations.json")
-
-
 def run_reference(args, dist):
+    """One complete FP64 MLMG solve (F-cycles, 2+2 Fsmooth, BiCGStab bottom,
+    ||r||_inf <= 1e-8 ||b||_inf) of the same 257^3 system by the oracle on
+    every host core, measured, not extrapolated.  The K timed steps together
+    run that one solve: step 0 does prepareForSolve, and each step runs up to
+    ceil(60 / K) iterations (the last one runs on to convergence), so the
+    whole solve lies inside the timed region.  value = the solve's wall time;
+    ms_per_step = value / K.  Each of the W warm-up steps is one F-cycle
+    iteration of a throw-away solve of the same system."""
     if dist.rank != 0:
         dist.close()
         return
-    import numpy as np
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     O.build()
     n = args.n
-    try:
-        with open(ITERATIONS_FILE) as f:
-            iters = int(json.load(f)["plain_fp64_iterations"])
-    except Exception:
-        iters = None
     ddw_h, bc = workload(n, args.grains)
     g = O.make_grid([n] * 3, sym=O.MAJORMINOR, bc_type=bc.type, bc_val=bc.val)
     N = O.nodes(g)
     b = O.bc_init(g, np.zeros(3 * N))
     rhs = O.newton_rhs(g, ddw_h, None, np.zeros(3 * N), b)
-    p1 = O.default_params(max_iter=1)
-
-    def step():
-        _, rep = O.solve(g, ddw_h, rhs, tol_rel=1e-8, tol_abs=0.0, params=p1)
-        return rep
-
-    for _ in range(args.warmup):
-        step()
-    vals, reps = [], []
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        r = step()
-        reps.append(r)
-        vals.append(r.t_setup + (iters or 1) * r.t_iter)
-    wall = (time.perf_counter() - t0) / args.steps
+    if args.warmup > 0:
+        w = O.Session(g, ddw_h, rhs, tol_rel=1e-8, tol_abs=0.0)
+        w.iterate(args.warmup)
+        w.finish()
+        del w
+    steps = max(1, args.steps)
+    chunk = max(1, int(math.ceil(60.0 / steps)))
+    step_s = []
+    sess = None
+    for k in range(steps):
+        t0 = time.perf_counter()
+        if sess is None:
+            sess = O.Session(g, ddw_h, rhs, tol_rel=1e-8, tol_abs=0.0)
+        sess.iterate(chunk if k < steps - 1 else 1 << 20)
+        step_s.append(time.perf_counter() - t0)
+    x, rep = sess.finish()
     cores = O.lib().orc_num_threads()
-    v = statistics.mean(vals)
-    sample = ("oracle/ CPU restatement (FP64, OpenMP %d threads); each step = prepareForSolve + 1 F-cycle "
-              "iteration at 257^3 (mean %.2f s), scaled to a full solve by %s iterations"
-              % (cores, wall, iters if iters else "1 (iteration count unknown)"))
+    v = sum(step_s)
+    rel = rep.res_final / max(float(np.abs(rhs).max()), rep.res0)
+    sample = ("measured: one complete solve of the %d^3-node system by the oracle/ CPU restatement (FP64 MLMG "
+              "F-cycles, OpenMP %d threads) to %.2e relative residual in %d iterations (status %d), "
+              "prepareForSolve %.2f s + iterations %.2f s, split over %d timed steps"
+              % (n + 1, cores, rel, rep.iterations, rep.status, rep.t_setup, rep.t_iter, steps))
     line = {"metric": METRIC, "value": v, "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": v * 1000.0, "higher_is_better": False, "scaling": "weak",
+            "warmup": args.warmup, "ms_per_step": v * 1000.0 / steps, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Voronoi polycrystal)",
             "config": {"workload": WORKLOAD, "nodes": N, "method": "MLMG F-cycles, FP64, CPU"},
             "impl": "reference",
             "cpu_baseline": {"value": v, "unit": "s", "cores": cores, "kind": "port", "sample": sample},
-            "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "reference_solve": {"iterations": rep.iterations, "status": rep.status, "res_rel_final": rel,
+                                "setup_s": rep.t_setup, "iterations_s": rep.t_iter,
+                                "step_s": [round(t, 3) for t in step_s]}}
     print(json.dumps(line), flush=True)
     dist.close()
 

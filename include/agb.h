@@ -316,8 +316,9 @@ agb_status agb_learned_solve(agb_solver s, agb_learned net, double* sol, const d
 /* Allocation-free coarsest-level solve.  No counterpart in the reference: it
  * exists for callers that may not allocate device memory when they need a
  * bottom solve -- a host framework that owns all device memory through its
- * own arena and forbids cudaMalloc inside solver hooks, or code running while
- * a stream is captured.  It computes what the solve's bottom step computes
+ * own arena and forbids cudaMalloc inside solver hooks, or a time-stepping
+ * code that must not stall on cudaMalloc's implicit synchronisation in the
+ * middle of a step.  It computes what the solve's bottom step computes
  * (BiCGStab on the diagonally scaled system, then smoothing) for one box with
  * no periodic direction, without calling cudaMalloc, cudaFree or any
  * allocating routine: its work vectors live in a device array of the library
@@ -326,14 +327,17 @@ agb_status agb_learned_solve(agb_solver s, agb_learned net, double* sol, const d
  *   - All array arguments are DEVICE pointers in the unpadded reference
  *     layout: ddw coefficient-major (AGB_LAYOUT_SOA), diag / res / cor with the
  *     three components one after the other; *ret receives the BiCGStab code
- *     (0 converged, 1-4 breakdown, 8 not converged).
- *   - Larger boxes are rejected with AGB_BADARG.
+ *     (0 converged, 1-4 breakdown, 8 not converged).  res and cor must not
+ *     overlap (cor is written while res is read).
+ *   - Larger boxes, and any periodic BC type, are rejected with AGB_BADARG.
  *   - The work is queued on `stream` (a cudaStream_t; NULL = default stream)
  *     and the call returns without waiting: results are valid once that
  *     stream has been synchronized.
  *   - The first call on a device looks up the array's device address (once
  *     per device, with that device current); make that first call before any
- *     stream capture.
+ *     stream capture.  The address is kept for the life of the process: a
+ *     caller that resets a device (cudaDeviceReset) must not call this entry
+ *     point again in that process.
  *   - Every call shares the one array: calls whose work overlaps on the GPU
  *     (several streams, several host threads) race and corrupt each other.
  *     Each call writes every scratch element before reading it, so nothing

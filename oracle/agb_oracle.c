@@ -958,8 +958,9 @@ static int bottom_bicgstab(mg_t* m, int l, double* sol, const double* rhs)
     return ret;
 }
 
-/* MLMG::actualBottomSolve: cor = 0, BiCGStab, zero on failure, then smooth */
-static void mg_bottom(mg_t* m)
+/* MLMG::actualBottomSolve: cor = 0, BiCGStab, zero on failure, then smooth;
+ * returns the BiCGStab code */
+static int mg_bottom(mg_t* m)
 {
     const int l = m->L - 1;
     const long n3 = 3 * m->N[l];
@@ -969,6 +970,27 @@ static void mg_bottom(mg_t* m)
         for (long q = 0; q < n3; q++) m->cor[l][q] = 0.0;
     int nsm = (ret == 0) ? m->p->bottom_smooth : m->p->final_smooth;
     mg_smooth(m, l, m->cor[l], m->res[l], nsm);
+    return ret;
+}
+
+/* The bottom step of one level on its own: cor <- BiCGStab(res) + smoothing,
+ * as mg_bottom does on the coarsest level of a solve.  diag is the level's
+ * Diagonal; returns the BiCGStab code (0 converged, 1-4 breakdown, 8 not
+ * converged). */
+int orc_bottom_solve(const orc_grid* g, const double* ddw, const double* diag, const double* res, double* cor,
+                     const orc_solver_params* p)
+{
+    mg_t m;
+    memset(&m, 0, sizeof(m));
+    m.p = p;
+    m.L = 1;
+    m.g[0] = *g;
+    m.N[0] = orc_nnodes(g);
+    m.ddw[0] = (double*)ddw;
+    m.diag[0] = (double*)diag;
+    m.res[0] = (double*)res;
+    m.cor[0] = cor;
+    return mg_bottom(&m);
 }
 
 /* MLMG::mgVcycle(amrlev=0, mglev_top) */
@@ -1006,80 +1028,119 @@ static void mg_fcycle(mg_t* m)
     }
 }
 
+/* A solve in progress: the hierarchy after prepareForSolve, the right-hand
+ * side and the stopping target.  orc_solve = begin + iterate (to the end) +
+ * end; the split form lets a caller run the iterations of one solve in
+ * several timed pieces. */
+struct orc_session {
+    mg_t m;
+    orc_grid g;
+    const double* b;
+    double* bproj;
+    int sing;
+    double max_norm, target, norm;
+    orc_report rep;
+};
+
+orc_session* orc_solve_begin(const orc_grid* g, const double* ddw, const orc_solver_params* p, const double* x,
+                             const double* b, double tol_rel, double tol_abs)
+{
+    orc_session* s = (orc_session*)calloc(1, sizeof(orc_session));
+    mg_t* m = &s->m;
+    m->p = p;
+    s->g = *g;
+    const double t0 = omp_get_wtime();
+    m->L = orc_num_levels(g, p->max_coarsening_level);
+    const int nc = orc_ncoef(g->sym);
+    m->g[0] = *g;
+    for (int l = 1; l < m->L; l++) orc_coarsen(&m->g[l - 1], &m->g[l]);
+    for (int l = 0; l < m->L; l++) {
+        m->N[l] = orc_nnodes(&m->g[l]);
+        long n3 = 3 * m->N[l];
+        m->ddw[l] = (l == 0) ? (double*)ddw : (double*)malloc(sizeof(double) * nc * m->N[l]);
+        m->diag[l] = (double*)malloc(sizeof(double) * n3);
+        m->cor[l] = (double*)calloc(n3, sizeof(double));
+        m->res[l] = (double*)calloc(n3, sizeof(double));
+        m->rescor[l] = (double*)calloc(n3, sizeof(double));
+        m->hold[l] = (double*)calloc(n3, sizeof(double));
+    }
+    /* Operator<Node>::prepareForSolve, Operator.cpp:253-260 */
+    for (int l = 1; l < m->L; l++) orc_average_ddw(&m->g[l - 1], m->ddw[l - 1], m->ddw[l]);
+    for (int l = 0; l < m->L; l++) orc_diagonal(&m->g[l], m->ddw[l], m->diag[l]);
+
+    /* fully periodic box: solve with the zero-mean part of b (see remove_mean) */
+    s->sing = fully_periodic(g);
+    if (s->sing) {
+        s->bproj = (double*)malloc(sizeof(double) * 3 * m->N[0]);
+        memcpy(s->bproj, b, sizeof(double) * 3 * m->N[0]);
+        remove_mean(g, s->bproj);
+        b = s->bproj;
+    }
+    s->b = b;
+    orc_residual(&m->g[0], m->ddw[0], x, b, m->res[0]);
+    if (s->sing) remove_mean(g, m->res[0]);
+    const double resnorm0 = orc_norm_inf(g, m->res[0]);
+    const double rhsnorm0 = orc_norm_inf(g, b);
+    s->max_norm = (rhsnorm0 >= resnorm0) ? rhsnorm0 : resnorm0;
+    double rel = tol_rel > 1e-16 ? tol_rel : 1e-16;
+    s->target = tol_abs > rel * s->max_norm ? tol_abs : rel * s->max_norm;
+    s->rep.res0 = resnorm0;
+    s->rep.iterations = 0;
+    s->rep.nlevels = m->L;
+    s->rep.status = (resnorm0 <= s->target) ? 0 : 1;
+    s->rep.res_final = resnorm0;
+    s->norm = resnorm0;
+    s->rep.t_setup = omp_get_wtime() - t0;
+    return s;
+}
+
+int orc_solve_iterate(orc_session* s, double* x, int max_steps)
+{
+    mg_t* m = &s->m;
+    const orc_solver_params* p = m->p;
+    const double t1 = omp_get_wtime();
+    const long n3 = 3 * m->N[0];
+    for (int step = 0; step < max_steps && s->rep.status == 1 && s->rep.iterations < p->max_iter; step++) {
+        const int iter = s->rep.iterations;
+        if (iter < p->max_fmg_iter) mg_fcycle(m);
+        else mg_vcycle(m, 0);
+        for (long q = 0; q < n3; q++) x[q] += m->cor[0][q];
+        orc_residual(&m->g[0], m->ddw[0], x, s->b, m->res[0]);
+        if (s->sing) remove_mean(&s->g, m->res[0]);
+        s->norm = orc_norm_inf(&s->g, m->res[0]);
+        s->rep.iterations = iter + 1;
+        if (p->verbose)
+            fprintf(stderr, "oracle MLMG iter %d resid %.6e rel %.6e\n", iter + 1, s->norm, s->norm / s->max_norm);
+        if (s->norm != s->norm) { s->rep.status = 2; break; }
+        if (s->norm <= s->target) { s->rep.status = 0; break; }
+        if (p->fixed_iter > 0 && iter + 1 >= p->fixed_iter) { s->rep.status = 0; break; }
+    }
+    s->rep.res_final = s->norm;
+    s->rep.t_iter += omp_get_wtime() - t1;
+    return s->rep.status;
+}
+
+int orc_solve_end(orc_session* s, double* x, orc_report* rep)
+{
+    mg_t* m = &s->m;
+    if (s->sing) remove_mean(&s->g, x);   /* solution modulo rigid translation */
+    if (rep) *rep = s->rep;
+    const int st = s->rep.status;
+    for (int l = 0; l < m->L; l++) {
+        if (l > 0) free(m->ddw[l]);
+        free(m->diag[l]); free(m->cor[l]); free(m->res[l]); free(m->rescor[l]); free(m->hold[l]);
+    }
+    free(s->bproj);
+    free(s);
+    return st;
+}
+
 int orc_solve(const orc_grid* g, const double* ddw, const orc_solver_params* p,
               double* x, const double* b, double tol_rel, double tol_abs, orc_report* rep)
 {
-    mg_t m;
-    memset(&m, 0, sizeof(m));
-    m.p = p;
-    const double t0 = omp_get_wtime();
-    m.L = orc_num_levels(g, p->max_coarsening_level);
-    const int nc = orc_ncoef(g->sym);
-    m.g[0] = *g;
-    for (int l = 1; l < m.L; l++) orc_coarsen(&m.g[l - 1], &m.g[l]);
-    for (int l = 0; l < m.L; l++) {
-        m.N[l] = orc_nnodes(&m.g[l]);
-        long n3 = 3 * m.N[l];
-        m.ddw[l] = (l == 0) ? (double*)ddw : (double*)malloc(sizeof(double) * nc * m.N[l]);
-        m.diag[l] = (double*)malloc(sizeof(double) * n3);
-        m.cor[l] = (double*)calloc(n3, sizeof(double));
-        m.res[l] = (double*)calloc(n3, sizeof(double));
-        m.rescor[l] = (double*)calloc(n3, sizeof(double));
-        m.hold[l] = (double*)calloc(n3, sizeof(double));
-    }
-    /* Operator<Node>::prepareForSolve, Operator.cpp:253-260 */
-    for (int l = 1; l < m.L; l++) orc_average_ddw(&m.g[l - 1], m.ddw[l - 1], m.ddw[l]);
-    for (int l = 0; l < m.L; l++) orc_diagonal(&m.g[l], m.ddw[l], m.diag[l]);
-
-    /* fully periodic box: solve with the zero-mean part of b (see remove_mean) */
-    const int sing = fully_periodic(g);
-    double* bproj = NULL;
-    if (sing) {
-        bproj = (double*)malloc(sizeof(double) * 3 * m.N[0]);
-        memcpy(bproj, b, sizeof(double) * 3 * m.N[0]);
-        remove_mean(g, bproj);
-        b = bproj;
-    }
-    orc_residual(&m.g[0], m.ddw[0], x, b, m.res[0]);
-    if (sing) remove_mean(g, m.res[0]);
-    const double resnorm0 = orc_norm_inf(g, m.res[0]);
-    const double rhsnorm0 = orc_norm_inf(g, b);
-    const double max_norm = (rhsnorm0 >= resnorm0) ? rhsnorm0 : resnorm0;
-    double rel = tol_rel > 1e-16 ? tol_rel : 1e-16;
-    const double target = tol_abs > rel * max_norm ? tol_abs : rel * max_norm;
-    rep->res0 = resnorm0;
-    rep->iterations = 0;
-    rep->nlevels = m.L;
-    rep->status = 1;
-    double norm = resnorm0;
-    const double t1 = omp_get_wtime();
-    rep->t_setup = t1 - t0;
-    if (resnorm0 <= target) rep->status = 0;
-    else {
-        const long n3 = 3 * m.N[0];
-        for (int iter = 0; iter < p->max_iter; iter++) {
-            if (iter < p->max_fmg_iter) mg_fcycle(&m);
-            else mg_vcycle(&m, 0);
-            for (long q = 0; q < n3; q++) x[q] += m.cor[0][q];
-            orc_residual(&m.g[0], m.ddw[0], x, b, m.res[0]);
-            if (sing) remove_mean(g, m.res[0]);
-            norm = orc_norm_inf(g, m.res[0]);
-            rep->iterations = iter + 1;
-            if (p->verbose) fprintf(stderr, "oracle MLMG iter %d resid %.6e rel %.6e\n", iter + 1, norm, norm / max_norm);
-            if (norm != norm) { rep->status = 2; break; }
-            if (norm <= target) { rep->status = 0; break; }
-            if (p->fixed_iter > 0 && iter + 1 >= p->fixed_iter) { rep->status = 0; break; }
-        }
-    }
-    rep->res_final = norm;
-    if (sing) remove_mean(g, x);   /* solution modulo rigid translation */
-    rep->t_iter = omp_get_wtime() - t1;
-    for (int l = 0; l < m.L; l++) {
-        if (l > 0) free(m.ddw[l]);
-        free(m.diag[l]); free(m.cor[l]); free(m.res[l]); free(m.rescor[l]); free(m.hold[l]);
-    }
-    free(bproj);
-    return rep->status;
+    orc_session* s = orc_solve_begin(g, ddw, p, x, b, tol_rel, tol_abs);
+    orc_solve_iterate(s, x, p->max_iter);
+    return orc_solve_end(s, x, rep);
 }
 
 /* Newton::solve with one Newton iteration (linear models), Newton.H:279-358 */

@@ -119,6 +119,17 @@ void   orc_traction_xhi(const orc_grid* g, const double* ddw, const double* F0,
 int    orc_solve(const orc_grid* g, const double* ddw, const orc_solver_params* p,
                  double* x, const double* b, double tol_rel, double tol_abs,
                  orc_report* rep);
+/* orc_solve in pieces: begin (prepareForSolve + first residual), iterate
+ * (up to max_steps more MLMG iterations; returns the status so far: 0
+ * converged, 1 still running / max_iter reached, 2 NaN), end (frees the
+ * state, fills rep).  x must be the same array across the calls. */
+typedef struct orc_session orc_session;
+orc_session* orc_solve_begin(const orc_grid* g, const double* ddw, const orc_solver_params* p, const double* x,
+                             const double* b, double tol_rel, double tol_abs);
+int    orc_solve_iterate(orc_session* s, double* x, int max_steps);
+int    orc_solve_end(orc_session* s, double* x, orc_report* rep);
+int    orc_bottom_solve(const orc_grid* g, const double* ddw, const double* diag, const double* res,
+                        double* cor, const orc_solver_params* p);
 int    orc_newton_solve(const orc_grid* g, const double* ddw, const double* F0,
                         const orc_solver_params* p, double* u, const double* b,
                         double tol_rel, double tol_abs, orc_report* rep);

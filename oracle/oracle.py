@@ -101,6 +101,11 @@ def lib():
         L.orc_solve.argtypes = [g, d, P(Params), d, d, ctypes.c_double, ctypes.c_double, P(Report)]
         L.orc_newton_solve.argtypes = [g, d, d, P(Params), d, d, ctypes.c_double, ctypes.c_double,
                                        P(Report)]
+        L.orc_solve_begin.argtypes = [g, d, P(Params), d, d, ctypes.c_double, ctypes.c_double]
+        L.orc_solve_begin.restype = ctypes.c_void_p
+        L.orc_solve_iterate.argtypes = [ctypes.c_void_p, d, ctypes.c_int]
+        L.orc_solve_end.argtypes = [ctypes.c_void_p, d, P(Report)]
+        L.orc_bottom_solve.argtypes = [g, d, d, d, d, P(Params)]
         L.orc_cubic.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_double, d, d]
         L.orc_quat_to_rot.argtypes = [d, d]
         L.orc_default_params.argtypes = [P(Params)]
@@ -238,6 +243,40 @@ def solve(g, ddw, b, x0=None, tol_rel=1e-8, tol_abs=0.0, params=None):
     lib().orc_solve(ctypes.byref(g), _p(ddw), ctypes.byref(p), _p(x), _p(b), tol_rel, tol_abs,
                     ctypes.byref(rep))
     return x, rep
+
+
+class Session:
+    """orc_solve in pieces: prepareForSolve and the first residual at
+    construction, then iterate(k) runs up to k more MLMG iterations (returns
+    the status so far: 0 converged, 1 running or out of iterations, 2 NaN),
+    finish() returns (x, report).  Holds references to every array the C
+    side keeps a pointer to."""
+
+    def __init__(self, g, ddw, b, x0=None, tol_rel=1e-8, tol_abs=0.0, params=None):
+        if b.shape != (3 * nodes(g),) or ddw.size != ncoef(g) * nodes(g):
+            raise ValueError("field sizes do not match the grid")
+        self.g, self.ddw, self.b = g, ddw, b
+        self.x = np.zeros(3 * nodes(g)) if x0 is None else np.array(x0, dtype=np.float64, copy=True)
+        self.p = params or default_params()
+        self.h = lib().orc_solve_begin(ctypes.byref(g), _p(ddw), ctypes.byref(self.p), _p(self.x), _p(b),
+                                       tol_rel, tol_abs)
+
+    def iterate(self, k):
+        return lib().orc_solve_iterate(self.h, _p(self.x), int(k))
+
+    def finish(self):
+        rep = Report()
+        lib().orc_solve_end(self.h, _p(self.x), ctypes.byref(rep))
+        self.h = None
+        return self.x, rep
+
+
+def bottom_solve(g, ddw, diag, res, params=None):
+    """The coarsest-level step of a solve on one level: (cor, BiCGStab code)."""
+    cor = np.zeros(3 * nodes(g))
+    p = params or default_params()
+    ret = lib().orc_bottom_solve(ctypes.byref(g), _p(ddw), _p(diag), _p(res), _p(cor), ctypes.byref(p))
+    return cor, ret
 
 
 def newton_solve(g, ddw, F0, u, b, tol_rel=1e-8, tol_abs=0.0, params=None):

@@ -1,8 +1,12 @@
 """Extract the reference's known-answer data for the elastic path into
 tests/golden/solid_kat.json and tests/golden/eshelby_kat.json.
 
-Run here (where the reference tree is mounted); the JSON travels with the
-repository.  Sources (paths relative to the alamo tree):
+Run where the reference tree is available, giving its root as the only
+argument or in ALAMO_REFERENCE (there is no default path); the JSON travels
+with the repository:
+
+    python tests/golden/make_golden.py <alamo source tree>
+  Sources (paths relative to the alamo tree):
   tests/Solid/input, tests/Solid/test                 4^3 cells, tensiontest
                                                       uniaxial_stress, disp (0,1:0,0.01),
                                                       tolerance 1e-4
@@ -20,7 +24,9 @@ import json
 import os
 import sys
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("ALAMO_REFERENCE")
+if not REF:
+    sys.exit("usage: make_golden.py <alamo source tree>  (or set ALAMO_REFERENCE)")
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "solid_kat.json")
 OUT_ESHELBY = os.path.join(os.path.dirname(os.path.abspath(__file__)), "eshelby_kat.json")
 
