@@ -53,9 +53,10 @@ def parse():
     ap.add_argument("--cycle", default="F", choices=["F", "V"])
     ap.add_argument("--krylov", type=int, default=8,
                     help="c2, rve: stored directions of the flexible GCR over the FP32 cycle (0: the FP32 cycles alone)")
-    ap.add_argument("--workload", default="c2", choices=["c2", "rve", "learned"],
+    ap.add_argument("--workload", default="c2", choices=["c2", "rve", "learned", "sweep"],
                     help="c2: the 257^3 polycrystal (default); rve: batched periodic RVEs; learned: the learned "
-                         "correction trained on 64^3 RVEs and evaluated at 128^3 and 256^3")
+                         "correction trained on 64^3 RVEs and evaluated at 128^3 and 256^3; sweep: the finest-level "
+                         "operator kernels of the c2 system alone (Fapply, residual, Jacobi; FP32 and FP64)")
     ap.add_argument("--rves", type=int, default=512, help="rve workload: number of RVEs")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "f64"], help="rve workload")
     return ap.parse_args()
@@ -340,6 +341,37 @@ def oracle_check(n, ddw_h, bc, x, rhs):
     return float(np.abs(r).max() / np.abs(rhs).max())
 
 
+def run_sweep(args, dist):
+    """The finest-level operator kernels of the c2 system timed alone:
+    `--steps` back-to-back launches per kernel after one warm-up launch (each
+    launch reads more than L2 holds), CUDA events on the operator's stream.
+    GB/s from the algorithmic bytes per node (FP32 cubic: Fapply 108, residual
+    120, Jacobi 132; FP64: 216, 240, 264)."""
+    import torch
+    from alamo_gb300 import Elastic
+    torch.cuda.set_device(dist.local)
+    n = args.n
+    nodes = (n + 1) ** 3
+    ddw_h, bc = workload(n, args.grains)
+    op = Elastic([n] * 3, None, "majorminor")
+    op.SetBC(bc)
+    op.SetModel(torch.from_numpy(ddw_h).cuda())
+    del ddw_h
+    bpn = {("f32", 0): 108, ("f32", 1): 120, ("f32", 2): 132, ("f64", 0): 216, ("f64", 1): 240, ("f64", 2): 264}
+    out = {}
+    for prec in ("f32", "f64"):
+        for mode, name in ((0, "fapply"), (1, "residual"), (2, "jacobi")):
+            ms = op.time_sweep(0, prec, mode, max(1, args.steps))
+            out["%s_%s" % (name, prec)] = {"ms": round(ms, 4), "gbs": round(bpn[(prec, mode)] * nodes / ms / 1e6, 1)}
+    op.close()
+    peak, kind = measured_peak_hbm()
+    line = {"metric": "finest-level operator sweeps, GB/s (algorithmic bytes)", "workload": "sweep", "n": n,
+            "nodes": nodes, "peak_hbm_gbs": peak, "peak_kind": kind, "sweeps": out}
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    dist.close()
+
+
 def run_rve(args, dist):
     """Batched RVE homogenization: `--rves` periodic RVEs (edges 32-96 cells,
     diffuse ellipsoidal inclusions, contrast up to 100, uniform eigenstrain),
@@ -469,6 +501,8 @@ def main():
         return run_rve(args, dist)
     if args.workload == "learned":
         return run_learned(args, dist)
+    if args.workload == "sweep":
+        return run_sweep(args, dist)
     res, ddw_h, bc = run_ours(args, dist)
     peak, peak_kind = measured_peak_hbm()
     nodes = res["nodes"]

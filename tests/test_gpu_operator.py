@@ -122,3 +122,36 @@ def test_newton_rhs_stress_traction(gpu_lib):
     assert rel_err(op.Stress(u, F0), O.stress(g, ddw, F0, u)) < TOL64
     t = op.TractionXhi(u, F0)
     assert rel_err(t, O.traction_xhi(g, ddw, F0, u)) < 1e-12
+
+
+# FP32 interiors of large levels go to the TMA kernel: boxes whose x extent is
+# not a multiple of its 32-node tile, whose y interior is not a multiple of
+# its 8 rows, and whose k interior splits into several chunks.  The smoothing
+# check uses displacement rows only: with random traction and Neumann rows
+# some boundary diagonals are ~1/h while the interior ones are ~1/h^2, and two
+# sweeps from random data amplify FP32 rounding there by that ratio.
+BIG32 = [([100, 37, 45], [0.01, 1 / 37, 0.02], (0, 0, 0)), ([64, 20, 24], [1 / 64, 0.05, 1 / 24], (0, 0, 0))]
+
+
+@pytest.mark.parametrize("case", BIG32)
+@pytest.mark.parametrize("sym", SYMS)
+@pytest.mark.parametrize("uniform", [False, True])
+def test_fp32_interior_apply_and_smooth(gpu_lib, case, sym, uniform):
+    op, g, ddw = make(case, sym, 11)
+    if uniform:
+        op.SetUniform(True)
+        g.uniform = 1
+    d32 = ddw.astype(np.float32).astype(np.float64)
+    u32 = random_field(case[0], 12, case[2], dtype=np.float32)
+    ref = O.fapply(g, d32, u32.astype(np.float64))
+    assert rel_err(op.Fapply(0, u32).astype(np.float64), ref) < TOL32
+    op.close()
+    op, g, ddw = make(case, sym, 11, ("disp",))
+    if uniform:
+        op.SetUniform(True)
+        g.uniform = 1
+    d32 = ddw.astype(np.float32).astype(np.float64)
+    b32 = random_field(case[0], 13, case[2], dtype=np.float32)
+    x = op.Fsmooth(0, u32.copy(), b32)
+    xs = O.fsmooth(g, d32, O.diagonal(g, d32), u32.astype(np.float64), b32.astype(np.float64))
+    assert rel_err(x.astype(np.float64), xs) < TOL32

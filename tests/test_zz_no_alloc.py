@@ -25,7 +25,7 @@ import oracle as O
 pytestmark = pytest.mark.gpu
 
 TOL = 1e-12          # against the existing entry point (same kernel, same rounding)
-TOL_ORACLE = 1e-8    # against the oracle (FP64 BiCGStab with another summation order)
+TOL_ORACLE = 1e-7    # against the oracle's converged (1e-12) bottom solve
 
 
 def problem(n):
@@ -117,10 +117,14 @@ def test_noalloc_rejects_periodic_and_in_place(gpu_lib):
     assert call_noalloc(n, zc, z, z, Constant(), default_params(), z, r) == AGB_BADARG
 
 
-def test_noalloc_bottom_matches_oracle_cubic(gpu_lib):
-    """A cubic (MajorMinor) polycrystal box with TensionTest rows: the
-    allocation-free bottom solve against the oracle's bottom step on the same
-    residual, twice in a row."""
+@pytest.mark.parametrize("tol", [1e-4, 1e-12])
+def test_noalloc_bottom_matches_oracle_cubic(gpu_lib, tol):
+    """A cubic (MajorMinor) polycrystal box with TensionTest rows, twice in a
+    row.  At the default bottom tolerance (1e-4) two BiCGStab runs that sum
+    in different orders stop on different iterates, so the check is the
+    oracle's residual of the GPU correction (the diagonally scaled residual
+    reduced by the tolerance); at 1e-12 both runs converge to the solution of
+    the same system and the corrections agree with the oracle's."""
     torch = pytest.importorskip("torch")
     from alamo_gb300 import default_params
     from alamo_gb300 import microstructure as M
@@ -133,7 +137,8 @@ def test_noalloc_bottom_matches_oracle_cubic(gpu_lib):
     g = O.make_grid([n] * 3, sym=O.MAJORMINOR, bc_type=bc.type, bc_val=bc.val)
     diag = O.diagonal(g, ddw)
     res = np.random.default_rng(5).uniform(-1, 1, 3 * N)
-    ref, ret_o = O.bottom_solve(g, ddw, diag, res)
+    params = default_params(bottom_tol_rel=tol, bottom_max_iter=400)
+    ref, ret_o = O.bottom_solve(g, ddw, diag, res, O.default_params(bottom_tol_rel=tol, bottom_max_iter=400))
     ddw_soa = np.ascontiguousarray(ddw.reshape(N, 21).T).reshape(-1)
     d_ddw = torch.from_numpy(ddw_soa).cuda()
     d_diag = torch.from_numpy(diag).cuda()
@@ -141,8 +146,14 @@ def test_noalloc_bottom_matches_oracle_cubic(gpu_lib):
     d_ret = torch.full((1,), -1, dtype=torch.int32, device="cuda")
     for call in range(2):
         d_out = torch.full((3 * N,), float("nan"), dtype=torch.float64, device="cuda")
-        check(call_noalloc(n, d_ddw, d_diag, d_res, bc, default_params(), d_out, d_ret, sym=AGB_MAJORMINOR))
+        check(call_noalloc(n, d_ddw, d_diag, d_res, bc, params, d_out, d_ret, sym=AGB_MAJORMINOR))
         torch.cuda.synchronize()
-        assert int(d_ret.item()) == ret_o, (call, int(d_ret.item()), ret_o)
-        err = np.abs(d_out.cpu().numpy() - ref).max() / np.abs(ref).max()
-        assert err < TOL_ORACLE, (call, err)
+        assert int(d_ret.item()) == ret_o == 0, (call, int(d_ret.item()), ret_o)
+        cor = d_out.cpu().numpy()
+        r = O.residual(g, ddw, cor, res)
+        # (the recursively updated BiCGStab residual drifts from the true one
+        # near 1e-12, so the true residual is held to 1e-10 there)
+        assert np.abs(r / diag).max() <= max(tol, 1e-10) * np.abs(res / diag).max() * 1.001, call
+        if tol < 1e-10:
+            err = np.abs(cor - ref).max() / np.abs(ref).max()
+            assert err < TOL_ORACLE, (call, err)
