@@ -114,6 +114,7 @@ def lib():
                                   ctypes.POINTER(AgbSolveReport)]),
         "agb_stress": (st, [vp, vp, vp, vp, ctypes.c_int]),
         "agb_traction_xhi": (st, [vp, vp, vp, dp, ctypes.c_int]),
+        "agb_strain_energy": (st, [vp, vp, vp, vp, ctypes.c_int]),
         "agb_op_time_sweep": (st, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]),
         "agb_host_alloc": (st, [ctypes.c_size_t, ctypes.POINTER(vp)]),
         "agb_host_free": (st, [vp]),

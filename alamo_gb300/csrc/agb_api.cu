@@ -1608,6 +1608,28 @@ agb_status agb_stress(agb_op op, const double* F0, const double* u, double* sigm
     return st;
 }
 
+agb_status agb_strain_energy(agb_op op, const double* u, double* eps9, double* energy, int mem)
+{
+    if (!op || !u || (!eps9 && !energy)) return fail(AGB_BADARG, "null argument");
+    if (!op->model_set) return fail(AGB_STATE, "SetModel must be called first");
+    Level& v = op->lev[0];
+    double *de = nullptr, *dw = nullptr;
+    agb_status st = AGB_OK;
+    if (eps9) st = op->alloc(&de, 9 * (size_t)v.L.S);
+    if (st == AGB_OK && energy) st = op->alloc(&dw, (size_t)v.L.S);
+    if (st == AGB_OK) st = upload<double, double>(op, v.L, 3, false, u, mem, v.hold64);
+    if (st == AGB_OK) {
+        launch_strain_energy(op->st, op->sym, v.L, v.ddw64, v.hold64, de, dw);
+        if (cudaGetLastError() != cudaSuccess) st = fail(AGB_CUDA, "strain/energy launch failed");
+    }
+    if (st == AGB_OK && eps9) st = download<double, double>(op, v.L, 9, true, de, eps9, mem);
+    if (st == AGB_OK && energy) st = download<double, double>(op, v.L, 1, false, dw, energy, mem);
+    if (st == AGB_OK && cudaStreamSynchronize(op->st) != cudaSuccess) st = fail(AGB_CUDA, "strain/energy failed");
+    if (de) release(op, de);
+    if (dw) release(op, dw);
+    return st;
+}
+
 agb_status agb_traction_xhi(agb_op op, const double* F0, const double* u, double trac[3], int mem)
 {
     if (!op || !u || !trac) return fail(AGB_BADARG, "null argument");

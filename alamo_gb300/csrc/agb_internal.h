@@ -247,6 +247,8 @@ void launch_newton_rhs(cudaStream_t st, int sym, const LevelDesc& L, const BCTab
                        const double* F0, const double* u, const double* b, double* rhs, double* dw_work);
 void launch_stress(cudaStream_t st, int sym, const LevelDesc& L, const double* ddw, const double* F0,
                    const double* u, double* sigma);
+void launch_strain_energy(cudaStream_t st, int sym, const LevelDesc& L, const double* ddw, const double* u,
+                          double* eps, double* energy);
 void launch_traction_xhi(cudaStream_t st, const LevelDesc& L, const double* sigma, double* out3);
 void launch_bc_init(cudaStream_t st, const LevelDesc& L, const BCTable& bc, double* rhs, int homogeneous);
 

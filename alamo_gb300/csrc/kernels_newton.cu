@@ -8,6 +8,8 @@
 //                 Newton.H:199-231
 //   bc_init       BC values into the RHS, BC/Operator/Elastic/Constant.H:100-194
 //   traction_xhi  trac_hi[0] face integral, Integrator/Base/Mechanics.H:391-431
+//   strain        eps = (grad u + grad u^T) / 2, Operator/Elastic.cpp:447-490
+//   energy        W = sig : eps / 2 with sig = C : grad u, Operator/Elastic.cpp:552-597
 #include <cuda_runtime.h>
 
 #include "agb_internal.h"
@@ -79,6 +81,39 @@ __global__ void k_dw(LevelDesc L, const double* __restrict__ ddw, const double* 
     c_mul_mat<double, SYM>(c, E, D);
     for (int r = 0; r < 3; r++)
         for (int s = 0; s < 3; s++) dw[(r * 3 + s) * L.S + a.base] = D[r][s];
+}
+
+// Elastic::Strain (non-Voigt, 9 per node, row-major) and Elastic::Energy per
+// node, with the gradient stencils of Numeric::GetStencil (one-sided on the
+// boundary).  Either output may be null.
+template <int SYM>
+__global__ void k_strain_energy(LevelDesc L, const double* __restrict__ ddw, const double* __restrict__ u,
+                                double* __restrict__ eps, double* __restrict__ energy)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z;
+    if (i >= L.nn[0] || j >= L.nn[1] || k >= L.nn[2]) return;
+    NAcc a;
+    a.x = u;
+    int mn[3], mx[3];
+    node_setup(L, i, j, k, a, mn, mx);
+    double G[3][3], E[3][3];
+    gradient(a, L, mn, mx, G);
+    for (int r = 0; r < 3; r++)
+        for (int s = 0; s < 3; s++) E[r][s] = 0.5 * (G[r][s] + G[s][r]);
+    if (eps)
+        for (int r = 0; r < 3; r++)
+            for (int s = 0; s < 3; s++) eps[(r * 3 + s) * L.S + a.base] = E[r][s];
+    if (energy) {
+        double c[NCoef<SYM>::value], S[3][3];
+        for (int m = 0; m < NCoef<SYM>::value; m++) c[m] = ddw[m * L.S + a.base];
+        c_mul_mat<double, SYM>(c, G, S);
+        double w = 0.0;
+        for (int r = 0; r < 3; r++)
+            for (int s = 0; s < 3; s++) w += 0.5 * S[r][s] * E[r][s];
+        energy[a.base] = w;
+    }
 }
 
 __global__ void k_newton_rhs(LevelDesc L, BCTable bc, const double* __restrict__ u, const double* __restrict__ b,
@@ -177,6 +212,15 @@ void launch_stress(cudaStream_t st, int sym, const LevelDesc& L, const double* d
     dim3 blk(32, 4, 2);
     if (sym == SYM_ISO) k_dw<SYM_ISO><<<grid_of(L, blk), blk, 0, st>>>(L, ddw, F0, u, sigma);
     else k_dw<SYM_MM><<<grid_of(L, blk), blk, 0, st>>>(L, ddw, F0, u, sigma);
+    count_launch();
+}
+
+void launch_strain_energy(cudaStream_t st, int sym, const LevelDesc& L, const double* ddw, const double* u,
+                          double* eps, double* energy)
+{
+    dim3 blk(32, 4, 2);
+    if (sym == SYM_ISO) k_strain_energy<SYM_ISO><<<grid_of(L, blk), blk, 0, st>>>(L, ddw, u, eps, energy);
+    else k_strain_energy<SYM_MM><<<grid_of(L, blk), blk, 0, st>>>(L, ddw, u, eps, energy);
     count_launch();
 }
 

@@ -5,8 +5,10 @@
 // <plot_file>/<step, 5 digits>node holding
 //   Header                  the plotfile header ("HyperCLaw-V1.1": component
 //                           names, geometry, level and grid extents)
-//   Level_0/Cell_H          the FabArray header of the level (one nodal box,
-//                           per-component minima and maxima)
+//   Level_0/Cell_H          the FabArray header of the level (VisMF header
+//                           version 1, written "NFiles"; one nodal box;
+//                           per-component minima and maxima in scientific
+//                           notation with 16 digits after the point)
 //   Level_0/Cell_D_00000    one FAB: a text header line, then the components
 //                           one after the other as little-endian IEEE doubles,
 //                           i fastest over the (n+1)^3 nodes
@@ -149,12 +151,12 @@ extern "C" agb_status agb_write_node_plotfile(const char* plot_file, int step, d
             set_error("agb_write_node_plotfile: cannot write Cell_H");
             return AGB_BADARG;
         }
-        fprintf(h, "1\n0\n%d\n0\n(1 0\n%s\n)\n1\nFabOnDisk: Cell_D_00000 0\n\n", nc, nodebox.c_str());
+        fprintf(h, "1\n1\n%d\n0\n(1 0\n%s\n)\n1\nFabOnDisk: Cell_D_00000 0\n\n", nc, nodebox.c_str());
         fprintf(h, "1,%d\n", nc);
-        for (int c = 0; c < nc; c++) fprintf(h, "%.17g,", mn[c]);
-        fprintf(h, "\n1,%d\n", nc);
-        for (int c = 0; c < nc; c++) fprintf(h, "%.17g,", mx[c]);
-        fprintf(h, "\n");
+        for (int c = 0; c < nc; c++) fprintf(h, "%.16e,", mn[c]);
+        fprintf(h, "\n\n1,%d\n", nc);
+        for (int c = 0; c < nc; c++) fprintf(h, "%.16e,", mx[c]);
+        fprintf(h, "\n\n");
         fclose(h);
     }
     // FAB

@@ -290,6 +290,15 @@ class Elastic:
         check(lib().agb_stress(self.h, _ptr(F0)[0], _ptr(u)[0], po, mem))
         return out
 
+    def StrainEnergy(self, u, strain=True, energy=True):
+        """Elastic::Strain (9 per node, row-major, AoS) and Elastic::Energy (1
+        per node) of u; returns (eps or None, energy or None)."""
+        eps = np.zeros(9 * self.nodes(0)) if strain else None
+        w = np.zeros(self.nodes(0)) if energy else None
+        pu, mem = _ptr(u)
+        check(lib().agb_strain_energy(self.h, pu, _ptr(eps)[0], _ptr(w)[0], mem))
+        return eps, w
+
     def TractionXhi(self, u, F0=None):
         t = (ctypes.c_double * 3)()
         pu, mem = _ptr(u)

@@ -80,8 +80,10 @@ def read_node_plotfile(path):
     fab_box = _box(h[5])
     m = re.match(r"FabOnDisk: (\S+) (\d+)", h[8])
     fab_file, fab_off = m.group(1), int(m.group(2))
-    mins = [float(v) for v in h[11].rstrip(",").split(",")]
-    maxs = [float(v) for v in h[13].rstrip(",").split(",")]
+    # two blocks "nfabs,ncomp" + one line of values each: minima, then maxima
+    blocks = [i for i in range(9, len(h)) if re.match(r"^\d+,\d+$", h[i])]
+    mins = [float(v) for v in h[blocks[0] + 1].rstrip(",").split(",")]
+    maxs = [float(v) for v in h[blocks[1] + 1].rstrip(",").split(",")]
     with open(os.path.join(path, os.path.dirname(mf_prefix), fab_file), "rb") as f:
         f.seek(fab_off)
         head = f.readline().decode()

@@ -179,6 +179,13 @@ agb_status agb_newton_solve(agb_solver s, const double* F0, double* u, const dou
                             double tol_abs, int mem, agb_solve_report* report);
 agb_status agb_stress(agb_op op, const double* F0, const double* u, double* sigma9, int mem);
 agb_status agb_traction_xhi(agb_op op, const double* F0, const double* u, double trac[3], int mem);
+/* Elastic::Strain(amrlev, eps, u, voigt = false), Operator/Elastic.cpp:428-490:
+ * eps9 = (grad u + grad u^T)/2, 9 per node, row-major, AoS (may be NULL);
+ * Elastic::Energy(amrlev, energy, u), Elastic.cpp:552-597: energy = sig : eps
+ * / 2 per node with sig = C : grad u (may be NULL; the reference adds this to
+ * the values already in its output field, this call writes it).  Gradients
+ * one-sided on the boundary as Numeric::GetStencil gives them. */
+agb_status agb_strain_energy(agb_op op, const double* u, double* eps9, double* energy, int mem);
 
 /* Batched RVE homogenization: `nprob` independent boxes (sizes n_cells[3*q..],
  * cell sizes dx[3*q..]; periodic in the directions of `periodic`, NULL = all)

@@ -762,6 +762,33 @@ void orc_stress(const orc_grid* g, const double* ddw, const double* F0, const do
             }
 }
 
+/* Elastic::Strain (voigt = false) and Elastic::Energy, Operator/Elastic.cpp:428-490,
+ * 552-597: eps = (grad u + grad u^T)/2 (9 per node, row-major) and W = sig : eps / 2
+ * with sig = C : grad u; either output may be NULL */
+void orc_strain_energy(const orc_grid* g, const double* ddw, const double* u, double* eps9, double* energy)
+{
+    const long N = orc_nnodes(g);
+#pragma omp parallel for schedule(static)
+    for (int k = 0; k <= g->n[2]; k++)
+        for (int j = 0; j <= g->n[1]; j++)
+            for (int i = 0; i <= g->n[0]; i++) {
+                double gu[3][3], sig[3][3], e[3][3];
+                node_dw(g, N, ddw, NULL, u, i, j, k, gu, sig);
+                for (int a = 0; a < 3; a++)
+                    for (int b = 0; b < 3; b++) e[a][b] = 0.5 * (gu[a][b] + gu[b][a]);
+                const long p = IDX(g, i, j, k);
+                if (eps9)
+                    for (int a = 0; a < 3; a++)
+                        for (int b = 0; b < 3; b++) eps9[p * 9 + a * 3 + b] = e[a][b];
+                if (energy) {
+                    double w = 0.0;
+                    for (int a = 0; a < 3; a++)
+                        for (int b = 0; b < 3; b++) w += 0.5 * sig[a][b] * e[a][b];
+                    energy[p] = w;
+                }
+            }
+}
+
 /* trac_hi[0] integral over the xhi face, Integrator/Base/Mechanics.H:391-431 */
 void orc_traction_xhi(const orc_grid* g, const double* ddw, const double* F0, const double* u, double trac[3])
 {

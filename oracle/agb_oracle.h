@@ -128,6 +128,7 @@ orc_session* orc_solve_begin(const orc_grid* g, const double* ddw, const orc_sol
                              const double* b, double tol_rel, double tol_abs);
 int    orc_solve_iterate(orc_session* s, double* x, int max_steps);
 int    orc_solve_end(orc_session* s, double* x, orc_report* rep);
+void   orc_strain_energy(const orc_grid* g, const double* ddw, const double* u, double* eps9, double* energy);
 int    orc_bottom_solve(const orc_grid* g, const double* ddw, const double* diag, const double* res,
                         double* cor, const orc_solver_params* p);
 int    orc_newton_solve(const orc_grid* g, const double* ddw, const double* F0,

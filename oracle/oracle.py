@@ -105,6 +105,7 @@ def lib():
         L.orc_solve_begin.restype = ctypes.c_void_p
         L.orc_solve_iterate.argtypes = [ctypes.c_void_p, d, ctypes.c_int]
         L.orc_solve_end.argtypes = [ctypes.c_void_p, d, P(Report)]
+        L.orc_strain_energy.argtypes = [g, d, d, d, d]
         L.orc_bottom_solve.argtypes = [g, d, d, d, d, P(Params)]
         L.orc_cubic.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_double, d, d]
         L.orc_quat_to_rot.argtypes = [d, d]
@@ -220,6 +221,14 @@ def newton_rhs(g, ddw, F0, u, b):
     rhs = np.zeros(3 * nodes(g))
     lib().orc_newton_rhs(ctypes.byref(g), _p(ddw), _p(F0), _p(u), _p(b), _p(rhs))
     return rhs
+
+
+def strain_energy(g, ddw, u):
+    """(eps 9 per node AoS, energy 1 per node)"""
+    e = np.zeros(9 * nodes(g))
+    w = np.zeros(nodes(g))
+    lib().orc_strain_energy(ctypes.byref(g), _p(ddw), _p(u), _p(e), _p(w))
+    return e, w
 
 
 def traction_xhi(g, ddw, F0, u):

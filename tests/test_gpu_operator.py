@@ -124,6 +124,20 @@ def test_newton_rhs_stress_traction(gpu_lib):
     assert rel_err(t, O.traction_xhi(g, ddw, F0, u)) < 1e-12
 
 
+@pytest.mark.parametrize("sym", SYMS)
+@pytest.mark.parametrize("per", [(0, 0, 0), (1, 0, 1)])
+def test_strain_energy(gpu_lib, sym, per):
+    n = [12, 10, 14]
+    op, g, ddw = make((n, [1 / 12, 0.1, 1 / 14], per), sym, 19)
+    u = random_field(n, 20, per)
+    e, w = op.StrainEnergy(u)
+    eo, wo = O.strain_energy(g, ddw, u)
+    assert rel_err(e, eo) < TOL64
+    assert rel_err(w, wo) < TOL64
+    e2, w2 = op.StrainEnergy(u, energy=False)
+    assert w2 is None and np.array_equal(e2, e)
+
+
 # FP32 interiors of large levels go to the TMA kernel: boxes whose x extent is
 # not a multiple of its 32-node tile, whose y interior is not a multiple of
 # its 8 rows, and whose k interior splits into several chunks.  The smoothing

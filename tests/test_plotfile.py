@@ -57,3 +57,72 @@ def test_node_plotfile_rejects_bad_fields(tmp_path):
         write_node_plotfile(tmp_path, 0, 0.0, n, [("bad", np.zeros(2 * 27))])
     with pytest.raises(ValueError):
         write_node_plotfile(tmp_path, 0, 0.0, n, [("short", np.zeros(26))])
+
+
+# The files AMReX's WriteMultiLevelPlotfile writes for a one-level, one-box
+# nodal MultiFab (what Integrator::WritePlotFile calls, Integrator.cpp:1022),
+# restated by hand from AMReX's plotfile layout (WriteGenericPlotfileHeader;
+# VisMF header version 1 written "NFiles", minima and maxima in scientific
+# notation with 16 digits after the point; the FAB header of a little-endian
+# IEEE double FAB): a 2 x 1 x 1-cell box on [0,1] x [0,0.5] x [0,0.5] at time
+# 0.25, step 3, one 3-component field "disp".
+GOLDEN_HEADER = """HyperCLaw-V1.1
+3
+disp_x
+disp_y
+disp_z
+3
+0.25
+0
+0 0 0 
+1 0.5 0.5 
+
+((0,0,0) (1,0,0) (0,0,0)) 
+3 
+0.5 0.5 0.5 
+0
+0
+0 1 0.25
+3
+0 1
+0 0.5
+0 0.5
+Level_0/Cell
+"""
+GOLDEN_CELL_H = """1
+1
+3
+0
+(1 0
+((0,0,0) (2,1,1) (1,1,1))
+)
+1
+FabOnDisk: Cell_D_00000 0
+
+1,3
+0.0000000000000000e+00,-2.7500000000000000e+00,1.0000000000000000e+00,
+
+1,3
+5.5000000000000000e+00,0.0000000000000000e+00,1.0000000000000000e+00,
+
+"""
+GOLDEN_FAB_HEAD = b"FAB ((8, (64 11 52 0 1 12 0 1023)),(8, (8 7 6 5 4 3 2 1)))((0,0,0) (2,1,1) (1,1,1)) 3\n"
+
+
+def test_node_plotfile_matches_amrex_layout(tmp_path):
+    from alamo_gb300 import build
+    build.build()
+    from alamo_gb300.plotfile import write_node_plotfile
+    n = (2, 1, 1)
+    N = 12
+    ux = 0.5 * np.arange(N)
+    uy = 0.0 - 0.25 * np.arange(N)   # (+0.0 at node 0)
+    uz = np.ones(N)
+    d = write_node_plotfile(tmp_path, 3, 0.25, n, [("disp", np.concatenate([ux, uy, uz]))], (0.0, 0.0, 0.0),
+                            (1.0, 0.5, 0.5))
+    assert open(os.path.join(d, "Header")).read() == GOLDEN_HEADER
+    assert open(os.path.join(d, "Level_0", "Cell_H")).read() == GOLDEN_CELL_H
+    raw = open(os.path.join(d, "Level_0", "Cell_D_00000"), "rb").read()
+    assert raw[:len(GOLDEN_FAB_HEAD)] == GOLDEN_FAB_HEAD
+    body = np.frombuffer(raw[len(GOLDEN_FAB_HEAD):], dtype="<f8")
+    assert np.array_equal(body, np.concatenate([ux, uy, uz]))
