@@ -115,6 +115,10 @@ def lib():
         "agb_stress": (st, [vp, vp, vp, vp, ctypes.c_int]),
         "agb_traction_xhi": (st, [vp, vp, vp, dp, ctypes.c_int]),
         "agb_strain_energy": (st, [vp, vp, vp, vp, ctypes.c_int]),
+        "agb_conv3_tc_pack": (st, [ctypes.c_int, ctypes.c_int, vp, vp, vp]),
+        "agb_conv3_tc": (st, [ip, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int, ctypes.c_int, vp, vp, vp,
+                              ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp]),
+        "agb_conv3_tc_error": (st, [ctypes.POINTER(ctypes.c_int)]),
         "agb_op_time_sweep": (st, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]),
         "agb_host_alloc": (st, [ctypes.c_size_t, ctypes.POINTER(vp)]),
         "agb_host_free": (st, [vp]),

@@ -28,6 +28,7 @@
 
 #include "agb_internal.h"
 #include "stencil.cuh"
+#include "tma.cuh"
 
 namespace agb {
 
@@ -73,47 +74,6 @@ struct TmaAcc {
         return c0[(m * TH_Y + ty + dj) * TW + tx + di];
     }
 };
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect(uint32_t bar, uint32_t bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-
-// Bounded wait for the phase of parity `parity` to complete: false after
-// about 2^31 clock cycles (~1 s at 2 GHz) without completion.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
-{
-    const long long t0 = clock64();
-    while (true) {
-        uint32_t ok;
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-            "selp.u32 %0, 1, 0, p;\n\t}"
-            : "=r"(ok)
-            : "r"(bar), "r"(parity)
-            : "memory");
-        if (ok) return true;
-        if (clock64() - t0 > (1LL << 31)) return false;
-    }
-}
-
-__device__ __forceinline__ void tma_load4(uint32_t dst, const CUtensorMap* map, int x, int y, int z, int c,
-                                          uint32_t bar)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
-        "[%6];" ::"r"(dst),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(c), "r"(bar)
-        : "memory");
-}
 
 template <int SYM, int MODE>
 __global__ void __launch_bounds__(TT_X* TT_Y) k_stencil_tma(LevelDesc L, Geo<float> g, int uniform,

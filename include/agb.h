@@ -289,6 +289,23 @@ agb_status agb_relu_backward(long long count, const void* y, void* dy, void* str
 agb_status agb_adam_step(long long count, float* w, const float* g, float* m, float* v, void* w_bf16, float lr,
                          float beta1, float beta2, float eps, int step, void* stream);
 
+/* 3x3x3 convolution on the fifth-generation tensor cores (tcgen05.mma with
+ * the accumulator in tensor memory, halo lines brought by TMA), zero padding
+ * outside the box, any box size; no reference counterpart.  Fields are
+ * channels-last BF16 with channel stride in_cs / out_cs (multiples of 8):
+ * the call reads channels [in_c0, in_c0 + cin) and writes [out_c0, out_c0 +
+ * cout) (slice starts multiples of 8), so a concatenation of skip inputs is
+ * one buffer.  cin a multiple of 16, cout 16, 32, 48 or 64.  wp holds the
+ * weights packed by agb_conv3_tc_pack from [27][cout][cin] BF16 (27 cin cout
+ * elements); bias (FP32, cout) may be NULL; out FP32 when out_f32; ReLU when
+ * relu.  Device pointers, 16-byte aligned; queued on `stream`.
+ * agb_conv3_tc_error reports (and clears) a bounded wait of the kernel that
+ * ran out since the last call. */
+agb_status agb_conv3_tc_pack(int cin, int cout, const void* w, void* wp, void* stream);
+agb_status agb_conv3_tc(const int n[3], int cin, int cout, const void* in, int in_cs, int in_c0, const void* wp,
+                        const float* bias, void* out, int out_cs, int out_c0, int out_f32, int relu, void* stream);
+agb_status agb_conv3_tc_error(int* flag);
+
 /* Learned correction inside a flexible GCR solve (no reference counterpart).
  * The network is a stack of agb_conv3 layers (channels 16/32/48; the first
  * takes 16 channels, the last gives 16; hidden layers ReLU, the last linear)
