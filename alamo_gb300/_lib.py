@@ -115,25 +115,34 @@ def lib():
         "agb_stress": (st, [vp, vp, vp, vp, ctypes.c_int]),
         "agb_traction_xhi": (st, [vp, vp, vp, dp, ctypes.c_int]),
         "agb_strain_energy": (st, [vp, vp, vp, vp, ctypes.c_int]),
-        "agb_conv3_tc_pack": (st, [ctypes.c_int, ctypes.c_int, vp, vp, vp]),
+        "agb_conv3_tc_pack": (st, [ctypes.c_int, ctypes.c_int, vp, ctypes.c_int, ctypes.c_int, vp, vp]),
         "agb_conv3_tc": (st, [ip, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int, ctypes.c_int, vp, vp, vp,
                               ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp]),
         "agb_conv3_tc_error": (st, [ctypes.POINTER(ctypes.c_int)]),
         "agb_op_time_sweep": (st, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]),
         "agb_host_alloc": (st, [ctypes.c_size_t, ctypes.POINTER(vp)]),
         "agb_host_free": (st, [vp]),
-        "agb_conv3_forward": (st, [ip, ctypes.c_int, ctypes.c_int, vp, vp, vp, vp, ctypes.c_int, ctypes.c_int, vp]),
-        "agb_conv3_wgrad": (st, [ip, ctypes.c_int, ctypes.c_int, vp, vp, vp, vp, vp]),
         "agb_conv3_flip": (st, [ctypes.c_int, ctypes.c_int, vp, vp, vp]),
-        "agb_relu_backward": (st, [ctypes.c_longlong, vp, vp, vp]),
         "agb_adam_step": (st, [ctypes.c_longlong, vp, vp, vp, vp, vp, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                ctypes.c_float, ctypes.c_int, vp]),
-        "agb_learned_create": (st, [ctypes.c_int, ip, ip, ctypes.POINTER(ctypes.c_float),
-                                    ctypes.POINTER(ctypes.c_float), ctypes.POINTER(vp)]),
+        "agb_conv3_wgrad0": (st, [ip, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int,
+                                  ctypes.c_int, vp, vp, vp]),
+        "agb_grid_prolong": (st, [ip, ip, ctypes.c_int, vp, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int, ctypes.c_int,
+                                  ctypes.c_float, ctypes.c_float, vp]),
+        "agb_grid_prolong_t": (st, [ip, ip, ctypes.c_int, vp, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int,
+                                    ctypes.c_int, ctypes.c_float, ctypes.c_float, vp]),
+        "agb_axpby_mask": (st, [ctypes.c_longlong, ctypes.c_int, vp, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int,
+                                ctypes.c_int, vp, ctypes.c_int, ctypes.c_int, ctypes.c_float, vp, ctypes.c_int,
+                                ctypes.c_int, vp]),
+        "agb_unet_layers": (st, [ip, ip, ip]),
+        "agb_unet_acts": (st, [ip, ip]),
+        "agb_unet_create": (st, [ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float), ctypes.POINTER(vp)]),
+        "agb_unet_set_weights": (st, [vp, ctypes.POINTER(vp), ctypes.POINTER(vp), vp]),
+        "agb_unet_forward": (st, [vp, ip, ctypes.POINTER(vp), vp, vp]),
+        "agb_unet_features": (st, [vp, vp, ctypes.c_int, vp, dp]),
         "agb_learned_destroy": (st, [vp]),
-        "agb_learned_features": (st, [ip, vp, vp, ctypes.c_double, vp, vp]),
-        "agb_learned_solve": (st, [vp, vp, vp, vp, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
-                                   ctypes.POINTER(AgbSolveReport)]),
+        "agb_solver_set_learned": (st, [vp, vp, ctypes.c_double, ctypes.c_int]),
+        "agb_solver_learned_stats": (st, [vp, ip, ip, ip]),
         "agb_write_node_plotfile": (st, [ctypes.c_char_p, ctypes.c_int, ctypes.c_double, ip, dp, dp, ctypes.c_int,
                                          ctypes.POINTER(ctypes.c_char_p), ip, ctypes.POINTER(vp), ctypes.c_int]),
         "agb_gen_voronoi_cubic": (st, [ip, ctypes.c_int, dp, dp, vp, vp, ctypes.c_int, vp]),

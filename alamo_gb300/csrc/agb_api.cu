@@ -151,10 +151,14 @@ struct agb_solver_s {
     double* kdots = nullptr;
     cudaGraphExec_t gpre = nullptr;
     long long gpre_kernels = 0;
-    // flexible GCR (agb_learned_solve): stored directions and work vectors
-    std::vector<double*> gZ, gW;
-    double *gr = nullptr, *gz = nullptr, *gw = nullptr, *grv = nullptr, *ge = nullptr, *gt = nullptr;
-    double* gdot = nullptr;
+    // learned correction (agb_solver_set_learned): the network, the
+    // acceptance threshold and the count of consecutive rejections that
+    // switches it off for the rest of a solve; per-solve statistics
+    agb_learned net = nullptr;
+    double learned_min_gain = 0.01;
+    int learned_max_fail = 2;
+    bool learned_on = false;
+    int learned_tried = 0, learned_kept = 0, learned_fails = 0;
 };
 
 // ---------------------------------------------------------------------------
@@ -785,7 +789,7 @@ agb_status inner_gcr32(agb_solver s, double inner_tol, double* inorm_out, int* c
     }
     if (!s->kr) {
         TRY(op->alloc(&s->kr, (size_t)n));
-        TRY(op->alloc(&s->kdots, GCR_MAX + 2));
+        TRY(op->alloc(&s->kdots, GCR_MAX + 4));
     }
     cudaStream_t st = op->st;
     const bool sing = L.singular();
@@ -825,6 +829,55 @@ agb_status inner_gcr32(agb_solver s, double inner_tol, double* inorm_out, int* c
         if (s->p.verbose) fprintf(stderr, "agb mixed GCR inner %d resid32 %.3e\n", it + 1, inorm);
         if (std::isnan(inorm)) break;
         if (inorm <= inner_tol) break;
+        if (s->net && s->learned_on) {
+            // the learned direction on the residual the cycle left, kept only
+            // if it removes at least learned_min_gain of the weighted residual
+            // norm squared (after Gram-Schmidt against the stored directions)
+            if (k == m) k = 0;
+            float* zl = s->kZ[k];
+            float* wl = s->kW[k];
+            TRY(learned_direction(s->net, st, op->sym, L, s->kr, v0.ddw32, zl));
+            launch_stencil<float>(st, op->sym, MODE_APPLY, L, op->bc, op->uniform, v0.ddw32, zl, nullptr, nullptr, wl,
+                                  0.0f, nullptr);
+            CK(cudaMemsetAsync(s->kdots, 0, sizeof(double) * (GCR_MAX + 4), st));
+            if (k > 0) {
+                GcrVecs W, Z;
+                for (int i = 0; i < k; i++) {
+                    W.v[i] = s->kW[i];
+                    Z.v[i] = s->kZ[i];
+                }
+                launch_multidot_w(st, n, k, wl, W, v0.dinv32, s->kdots);
+                launch_gcr_orth(st, n, k, s->kdots, W, Z, wl, zl);
+            }
+            GcrVecs P;
+            P.v[0] = wl;
+            P.v[1] = s->kr;
+            launch_multidot_w(st, n, 2, wl, P, v0.dinv32, s->kdots + GCR_MAX);
+            GcrVecs R;
+            R.v[0] = s->kr;
+            launch_multidot_w(st, n, 1, s->kr, R, v0.dinv32, s->kdots + GCR_MAX + 2);
+            CK(cudaMemcpyAsync(op->h_slots + 4, s->kdots + GCR_MAX, 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            const double ww = op->h_slots[4], wr = op->h_slots[5], rr = op->h_slots[6];
+            const double gain = (ww > 0 && rr > 0) ? wr * wr / (ww * rr) : 0.0;
+            s->learned_tried++;
+            if (std::isfinite(gain) && gain >= s->learned_min_gain) {
+                CK(cudaMemsetAsync(op->d_slots + 1, 0, sizeof(double), st));
+                launch_gcr_step(st, n, s->kdots + GCR_MAX, wl, zl, s->sol32, s->kr, op->d_slots + 1);
+                CK(cudaMemcpyAsync(op->h_slots + 1, op->d_slots + 1, sizeof(double), cudaMemcpyDeviceToHost, st));
+                CK(cudaStreamSynchronize(st));
+                inorm = slot_as_float(op->h_slots, 1);
+                k++;
+                s->learned_kept++;
+                s->learned_fails = 0;
+                if (s->p.verbose) fprintf(stderr, "agb learned direction kept: gain %.3e resid32 %.3e\n", gain, inorm);
+                if (std::isnan(inorm)) break;
+                if (inorm <= inner_tol) break;
+            } else {
+                if (++s->learned_fails >= s->learned_max_fail) s->learned_on = false;
+                if (s->p.verbose) fprintf(stderr, "agb learned direction rejected: gain %.3e\n", gain);
+            }
+        }
         slow = (inorm > 0.9 * prev) ? slow + 1 : 0;
         if (slow >= 3) break;   // FP32 floor reached
         prev = inorm;
@@ -838,6 +891,8 @@ agb_status solve_mixed(agb_solver s, double tol_rel, double tol_abs, agb_solve_r
 {
     agb_op op = s->op;
     TRY(ensure_f32(op));
+    s->learned_on = s->net != nullptr && s->p.krylov > 0 && learned_level_ok(op->lev[0].L);
+    s->learned_tried = s->learned_kept = s->learned_fails = 0;
     Level& v0 = op->lev[0];
     double res0, bnorm;
     TRY(initial_residual(s, &res0));
@@ -887,6 +942,7 @@ agb_status solve_mixed(agb_solver s, double tol_rel, double tol_abs, agb_solve_r
         if (std::isnan(norm)) { st = AGB_NAN; break; }
         if (norm <= target) { st = AGB_OK; break; }
         no_progress = (norm > 0.5 * old) ? no_progress + 1 : 0;
+        if (no_progress >= 1) s->learned_on = false;   // the FP64 residual is the judge: plain cycles from here
         if (no_progress >= 2) { st = AGB_STALL; break; }
     }
     rep->iterations = total_cycles;
@@ -1308,166 +1364,42 @@ agb_status agb_solve(agb_solver s, double* sol, const double* rhs, double tol_re
 }
 
 // Flexible GCR with a V-cycle (+ learned correction) preconditioner; see agb.h.
-agb_status agb_learned_solve(agb_solver s, agb_learned net, double* sol, const double* rhs, double tol_rel,
-                             double tol_abs, int restart, int mem, agb_solve_report* report)
+agb_status agb_solver_set_learned(agb_solver s, agb_learned net, double min_gain, int max_fail)
 {
-    if (!s || !sol || !rhs) return fail(AGB_BADARG, "null argument");
-    if (restart < 1 || restart > 64) return fail(AGB_BADARG, "restart must be in 1..64");
-    agb_op op = s->op;
-    Level& v0 = op->lev[0];
-    const LevelDesc& L0 = v0.L;
-    if (net && (op->sym != AGB_ISO || !learned_box_ok(L0)))
-        return fail(AGB_BADARG, "the learned correction needs a fully periodic isotropic box with edges "
-                                "multiples of 16, 4 and 2");
-    const size_t n3 = 3 * (size_t)L0.S;
-    while ((int)s->gZ.size() < restart) {
-        double *z = nullptr, *w = nullptr;
-        TRY(op->alloc(&z, n3));
-        TRY(op->alloc(&w, n3));
-        s->gZ.push_back(z);
-        s->gW.push_back(w);
-    }
-    if (!s->gr) {
-        TRY(op->alloc(&s->gr, n3));
-        TRY(op->alloc(&s->gz, n3));
-        TRY(op->alloc(&s->gw, n3));
-        TRY(op->alloc(&s->grv, n3));
-        TRY(op->alloc(&s->ge, n3));
-        TRY(op->alloc(&s->gt, n3));
-        TRY(op->alloc(&s->gdot, 4));
-    }
-    agb_solve_report rep;
-    memset(&rep, 0, sizeof(rep));
-    const long long k0 = launch_counter();
-    cudaStream_t st = op->st;
-    CK(cudaEventRecord(op->e0, st));
-    op->prepared = false;
+    if (!s) return fail(AGB_BADARG, "null solver");
+    if (net && !learned_level_ok(s->op->lev[0].L))
+        return fail(AGB_BADARG, "the learned correction needs a box with no periodic direction and edges divisible by 4");
+    if (!(min_gain >= 0 && min_gain < 1) || max_fail < 1) return fail(AGB_BADARG, "min_gain in [0,1), max_fail >= 1");
+    s->net = net;
+    s->learned_min_gain = min_gain;
+    s->learned_max_fail = max_fail;
+    return AGB_OK;
+}
+
+agb_status agb_solver_learned_stats(agb_solver s, int* tried, int* kept, int* active)
+{
+    if (!s || !tried || !kept || !active) return fail(AGB_BADARG, "null argument");
+    *tried = s->learned_tried;
+    *kept = s->learned_kept;
+    *active = s->learned_on ? 1 : 0;
+    return AGB_OK;
+}
+
+agb_status agb_unet_features(agb_op op, const double* r, int mem, void* feat, double* rms)
+{
+    TRY(check_level(op, 0));
+    if (!r || !feat || !rms) return fail(AGB_BADARG, "null argument");
+    Level& v = op->lev[0];
+    if (!learned_level_ok(v.L))
+        return fail(AGB_BADARG, "the learned correction needs a box with no periodic direction and edges divisible by 4");
     TRY(prepare(op));
     TRY(ensure_f32(op));
-    TRY((upload<double, double>(op, L0, 3, false, sol, mem, s->x64)));
-    TRY((upload<double, double>(op, L0, 3, false, rhs, mem, s->b64)));
-    const bool sing = L0.singular();
-    if (sing) launch_remove_mean<double>(st, L0, s->b64, op->d_slots + 8);
-    const long long nall = (long long)n3;
-    // inner product weighted by 1/diag^2 (rows scaled to a unit diagonal, as in
-    // the mixed solve's inner GCR)
-    auto dot = [&](const double* a, const double* b, double* outv) -> agb_status {
-        CK(cudaMemsetAsync(s->gdot, 0, sizeof(double), st));
-        launch_dot(st, nall, a, b, s->gdot, v0.dinv64);
-        CK(cudaMemcpyAsync(op->h_slots + 12, s->gdot, sizeof(double), cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
-        *outv = op->h_slots[12];
-        return AGB_OK;
-    };
-    auto ninf = [&](const double* a, double* outv) { return norm64(op, L0, a, outv); };
-    Engine<double> E64{op, s->p};
-    Engine<float> E32{op, s->p};
-    // w = P A z (P the zero-mean projection on a fully periodic box)
-    auto apply = [&](const double* z, double* w) {
-        launch_stencil<double>(st, op->sym, MODE_APPLY, L0, op->bc, op->uniform, v0.ddw64, z, nullptr, nullptr, w,
-                               0.0, nullptr);
-        if (sing) launch_remove_mean<double>(st, L0, w, op->d_slots + 11);
-    };
-    // r = b - A x
-    CK(cudaMemsetAsync(op->d_slots, 0, sizeof(double), st));
-    E64.fine_residual(s->x64, s->b64, s->gr, op->d_slots);
-    double res0, bnorm;
-    TRY(ninf(s->gr, &res0));
-    TRY(ninf(s->b64, &bnorm));
-    const double target = std::max(tol_abs, std::max(tol_rel, 1e-16) * std::max(bnorm, res0));
-    rep.res0 = res0;
-    rep.rhs_norm = bnorm;
-    rep.nlevels = (int)op->lev.size();
-    double norm = res0;
-    agb_status status = AGB_MAXITER;
-    int m = 0, fallbacks = 0;
-    if (std::isnan(res0)) status = AGB_NAN;
-    else if (res0 <= target) status = AGB_OK;
-    else {
-        // Add the direction (z, w = P A z) to the GCR space: orthogonalise w
-        // against the stored directions (modified Gram-Schmidt), normalise,
-        // and minimise the residual over the new direction.
-        auto gcr_add = [&](double* z, double* w) -> agb_status {
-            if (m == restart) m = 0;   // restart
-            for (int i = 0; i < m; i++) {
-                double beta;
-                TRY(dot(w, s->gW[i], &beta));
-                launch_axpy<double>(st, L0, 3, w, s->gW[i], -beta);
-                launch_axpy<double>(st, L0, 3, z, s->gZ[i], -beta);
-            }
-            double ww;
-            TRY(dot(w, w, &ww));
-            if (!(ww > 0) || std::isnan(ww)) return std::isnan(ww) ? AGB_NAN : AGB_STALL;
-            const double inv = 1.0 / std::sqrt(ww);
-            launch_zero<double>(st, L0, 3, s->gW[m]);
-            launch_zero<double>(st, L0, 3, s->gZ[m]);
-            launch_axpy<double>(st, L0, 3, s->gW[m], w, inv);
-            launch_axpy<double>(st, L0, 3, s->gZ[m], z, inv);
-            double alpha;
-            TRY(dot(s->gr, s->gW[m], &alpha));
-            launch_axpy<double>(st, L0, 3, s->x64, s->gZ[m], alpha);
-            launch_axpy<double>(st, L0, 3, s->gr, s->gW[m], -alpha);
-            m++;
-            return AGB_OK;
-        };
-        for (int it = 0; it < s->p.max_iter; it++) {
-            // V-cycle direction: z = V(r), one FP32 V-cycle on r / ||r||
-            launch_convert<float, double>(st, L0, 3, s->gr, v0.res32, 1.0 / norm);
-            E32.vcycle(0);
-            launch_zero<double>(st, L0, 3, s->gz);
-            launch_axpy_mixed(st, L0, 3, s->gz, v0.cor32, norm);
-            apply(s->gz, s->gw);
-            agb_status gs = gcr_add(s->gz, s->gw);
-            if (gs != AGB_OK) { status = gs; break; }
-            rep.iterations = it + 1;
-            TRY(ninf(s->gr, &norm));
-            if (s->p.verbose)
-                fprintf(stderr, "agb GCR iter %d V-cycle direction: resid %.6e rel %.6e\n", it + 1, norm,
-                        norm / std::max(bnorm, res0));
-            if (std::isnan(norm)) { status = AGB_NAN; break; }
-            if (norm <= target) { status = AGB_OK; break; }
-            if (!net) continue;
-            // learned direction: e = N(r) on the residual the V-cycle direction left
-            double r2_before, r2_after;
-            TRY(dot(s->gr, s->gr, &r2_before));
-            const agb_status ls = learned_apply(net, st, L0, s->gr, v0.ddw64, s->ge);
-            if (ls != AGB_OK) return fail(ls, "learned correction failed");
-            apply(s->ge, s->gt);
-            gs = gcr_add(s->ge, s->gt);
-            if (gs == AGB_STALL) { fallbacks++; continue; }   // no new direction: the V-cycle carries on
-            if (gs != AGB_OK) { status = gs; break; }
-            TRY(dot(s->gr, s->gr, &r2_after));
-            if (!(r2_after < 0.99 * r2_before)) fallbacks++;   // the learned direction did not help
-            TRY(ninf(s->gr, &norm));
-            if (s->p.verbose)
-                fprintf(stderr, "agb GCR iter %d learned direction: resid %.6e (|r|_2 x %.3f)\n", it + 1, norm,
-                        std::sqrt(r2_after / std::max(r2_before, 1e-300)));
-            if (std::isnan(norm)) { status = AGB_NAN; break; }
-            if (norm <= target) { status = AGB_OK; break; }
-        }
-    }
-    // the true residual of the returned x
-    CK(cudaMemsetAsync(op->d_slots, 0, sizeof(double), st));
-    E64.fine_residual(s->x64, s->b64, s->gr, op->d_slots);
-    TRY(ninf(s->gr, &norm));
-    if (status == AGB_OK && norm > target * 1.0000001) status = AGB_MAXITER;
-    rep.res_final = norm;
-    rep.refinements = fallbacks;
-    if (sing) launch_remove_mean<double>(st, L0, s->x64, op->d_slots + 8);
-    TRY((download<double, double>(op, L0, 3, false, s->x64, sol, mem)));
-    CK(cudaEventRecord(op->e1, st));
-    CK(cudaStreamSynchronize(st));
-    float ms = 0;
-    cudaEventElapsedTime(&ms, op->e0, op->e1);
-    rep.solve_ms = ms;
-    rep.status = status;
-    rep.kernels = launch_counter() - k0;
-    if (report) *report = rep;
-    if (tma_error_take()) return fail(AGB_CUDA, "a TMA plane copy of the stencil kernel did not complete in time");
-    if (status != AGB_OK)
-        fail(status, "GCR did not converge: status %d after %d iterations, |r| %.3e", (int)status, rep.iterations,
-             rep.res_final);
-    return status;
+    TRY((upload<float, double>(op, v.L, 3, false, r, mem, v.hold32)));
+    TRY(learned_features(op->st, op->sym, v.L, v.hold32, v.ddw32, feat, op->d_slots + 4));
+    CK(cudaMemcpyAsync(op->h_slots + 4, op->d_slots + 4, sizeof(double), cudaMemcpyDeviceToHost, op->st));
+    CK(cudaStreamSynchronize(op->st));
+    *rms = std::sqrt(op->h_slots[4] / (3.0 * (double)v.L.count()));
+    return AGB_OK;
 }
 
 agb_status agb_apply(agb_solver s, double* out, const double* in, int mem)

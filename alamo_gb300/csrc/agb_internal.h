@@ -208,9 +208,19 @@ void launch_gcr_step(cudaStream_t st, long long n, const double* dots, float* w,
 void launch_dot(cudaStream_t st, long long n, const double* x, const double* y, double* out,
                 const double* w = nullptr);
 // learned correction network (learned.cu)
-bool learned_box_ok(const LevelDesc& L);
-agb_status learned_apply(agb_learned net, cudaStream_t st, const LevelDesc& L, const double* r, const double* ddw64,
-                         double* e);
+// learned correction (learned.cu): the U-Net direction z = N(r) of an FP32
+// residual on the finest level of a box (no periodic direction, edges
+// divisible by 4), queued on st without host synchronisation
+bool learned_level_ok(const LevelDesc& L);
+agb_status learned_direction(agb_learned net, cudaStream_t st, int sym, const LevelDesc& L, const float* r,
+                             const float* ddw32, float* z);
+agb_status learned_features(cudaStream_t st, int sym, const LevelDesc& L, const float* r, const float* ddw32,
+                            void* feat, double* acc);
+// nodal grid transfers of channels-last BF16 fields (kernels_conv.cu)
+void launch_prolong(cudaStream_t st, const int gf[3], const int gc[3], int C, const void* crs, int c_cs, int c_c0,
+                    void* fine, int f_cs, int f_c0, float beta, float s);
+void launch_prolong_t(cudaStream_t st, const int gf[3], const int gc[3], int C, const void* fine, int f_cs, int f_c0,
+                      void* crs, int c_cs, int c_c0, float beta, float s);
 // x -= per-component mean over the stored nodes (sums3: 3 doubles of scratch);
 // with norm_slot, also max |x| after the subtraction (atomic max into a zeroed slot)
 template <typename T>

@@ -237,8 +237,9 @@ __global__ void __launch_bounds__(TC_THREADS) k_conv3_tc(const __grid_constant__
                      : "memory");
 }
 
-// wp[((s * 27 + tap) * 2 + h) * cout + co][e] = w[tap][co][16 s + 8 h + e]
-__global__ void k_conv3_tc_pack(int cin, int cout, const __nv_bfloat16* __restrict__ w, __nv_bfloat16* __restrict__ wp)
+// wp[((s * 27 + tap) * 2 + h) * cout + co][e] = w[tap][co0 + co][16 s + 8 h + e], w of w_cout rows per tap
+__global__ void k_conv3_tc_pack(int cin, int cout, const __nv_bfloat16* __restrict__ w, int w_cout, int co0,
+                                __nv_bfloat16* __restrict__ wp)
 {
     const long long total = 27LL * cout * cin;
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
@@ -251,7 +252,7 @@ __global__ void k_conv3_tc_pack(int cin, int cout, const __nv_bfloat16* __restri
         r /= 2;
         const int tap = (int)(r % 27);
         const int s = (int)(r / 27);
-        wp[q] = w[((long long)tap * cout + co) * cin + 16 * s + 8 * h + e];
+        wp[q] = w[((long long)tap * w_cout + co0 + co) * cin + 16 * s + 8 * h + e];
     }
 }
 
@@ -332,15 +333,18 @@ int conv_tc_error_take()
 
 using namespace agb;
 
-extern "C" agb_status agb_conv3_tc_pack(int cin, int cout, const void* w, void* wp, void* stream)
+extern "C" agb_status agb_conv3_tc_pack(int cin, int cout, const void* w, int w_cout, int w_co0, void* wp,
+                                        void* stream)
 {
-    if (cin < 16 || cin % 16 || (cout != 16 && cout != 32 && cout != 48 && cout != 64) || !w || !wp) {
-        set_error("agb_conv3_tc_pack: cin must be a positive multiple of 16, cout 16, 32, 48 or 64");
+    if (cin < 16 || cin % 16 || (cout != 16 && cout != 32 && cout != 48 && cout != 64) || !w || !wp ||
+        w_co0 < 0 || w_co0 + cout > w_cout) {
+        set_error("agb_conv3_tc_pack: cin must be a positive multiple of 16, cout 16, 32, 48 or 64, rows inside w");
         return AGB_BADARG;
     }
     const long long total = 27LL * cout * cin;
     const int blocks = (int)std::min<long long>((total + 255) / 256, 8LL * sm_count());
-    k_conv3_tc_pack<<<blocks, 256, 0, (cudaStream_t)stream>>>(cin, cout, (const __nv_bfloat16*)w, (__nv_bfloat16*)wp);
+    k_conv3_tc_pack<<<blocks, 256, 0, (cudaStream_t)stream>>>(cin, cout, (const __nv_bfloat16*)w, w_cout, w_co0,
+                                                               (__nv_bfloat16*)wp);
     count_launch();
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {

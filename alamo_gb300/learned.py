@@ -1,22 +1,22 @@
-"""Learned correction for the multigrid-preconditioned GCR solve of periodic
-isotropic RVEs (agb_learned_* and agb_conv3_* in the C ABI).
+"""Learned correction for the mixed-precision multigrid solve (agb_unet_* and
+agb_solver_set_learned in the C ABI).  No counterpart in the reference.
 
-The network is a stack of 3x3x3 convolutions over the finest level, run by
-this project's BF16 implicit-GEMM kernels (forward, data and weight
-gradients) with Adam on FP32 master weights; torch tensors only hold device
-memory here.  It is trained to map the residual left by one V-cycle,
-r1 = r - A V(r), to the error that remains, e1 = A^{-1} r - V(r); inside
-agb_learned_solve every GCR iteration adds the V-cycle direction V(r) and
-then the learned direction N(r1) on the residual it left, and GCR minimises
-the residual over all stored directions (a learned direction that does not
-help leaves the V-cycle directions to carry the solve: the fallback).
+The network is the library's three-level convolutional encoder-decoder
+(channels 16/32/64, 3x3x3 convolutions on the tensor cores with zero padding,
+skip connections, full weighting down and trilinear prolongation up between
+nodal grids).  Its forward pass is the library's (agb_unet_forward, the same
+code the solver runs); the backward pass here chains the library's gradient
+kernels (weight gradients, data gradients as convolutions with flipped
+weights, grid transfers and their transposes, ReLU masks), and Adam updates
+FP32 master weights with BF16 copies.  torch tensors only hold device memory
+and compute the loss.
 
-    ConvNet        layers, forward/backward through the kernels, Adam, export
-    training_pairs samples (features, residual, error target) from solves of
-                   periodic RVEs
-    train          Adam on the error of the correction
-    train_highpass Adam on the high-frequency part of that error
-    LearnedSolver  agb_learned_solve with or without the network (ablation)
+    UNet             weights, forward, backward, Adam, attach to a solver
+    training_samples residuals and errors of multigrid iterates on random
+                     cubic polycrystals (the solves the plain multigrid makes)
+    train            Adam on the cosine between the network's correction and
+                     the error (GCR rescales every direction, so only the
+                     direction matters)
 """
 import ctypes
 
@@ -24,119 +24,66 @@ import numpy as np
 
 from . import _lib
 from ._lib import check, lib
-from .elastic import Elastic, Linear, _ptr, default_params
+from .elastic import Elastic, Linear, _ptr
 
 FEAT = 16
-DEFAULT_LAYERS = ((16, 32), (32, 32), (32, 16), (16, 16))   # (cin, cout); hidden ReLU, last linear
 
 
 def _vp(t):
     return ctypes.c_void_p(t.data_ptr()) if t is not None else None
 
 
-def _cells(n):
-    return (ctypes.c_int * 3)(*[int(v) for v in n])
+def _i3(g):
+    return (ctypes.c_int * 3)(*[int(v) for v in g])
 
 
-class ConvNet:
-    def __init__(self, layers=DEFAULT_LAYERS, seed=0):
+def topology():
+    L = lib()
+    nl, na = 11, 13
+    cin, cout, lev = (ctypes.c_int * nl)(), (ctypes.c_int * nl)(), (ctypes.c_int * nl)()
+    check(L.agb_unet_layers(cin, cout, lev))
+    alev, ach = (ctypes.c_int * na)(), (ctypes.c_int * na)()
+    check(L.agb_unet_acts(alev, ach))
+    return list(cin), list(cout), list(lev), list(alev), list(ach)
+
+
+def grids(g0):
+    return [tuple(((int(v) - 1) >> l) + 1 for v in g0) for l in range(3)]
+
+
+# activation indices (the order of agb_unet_acts)
+FEATS, A1, CAT0, P1, B1, CAT1, P2, C1, C2, D1, E1, F0, H0 = range(13)
+
+
+class UNet:
+    def __init__(self, seed=0):
         import torch
         self.torch = torch
-        self.layers = [tuple(int(v) for v in l) for l in layers]
-        if self.layers[0][0] != FEAT or self.layers[-1][1] != FEAT:
-            raise ValueError("the first layer takes %d channels and the last gives %d" % (FEAT, FEAT))
+        self.cin, self.cout, self.lev, self.alev, self.ach = topology()
         g = torch.Generator().manual_seed(seed)
-        self.w, self.b, self.wb, self.mw, self.vw, self.mb, self.vb = [], [], [], [], [], [], []
-        for l, (ci, co) in enumerate(self.layers):
+        self.w, self.b, self.wb = [], [], []
+        self.mw, self.vw, self.mb, self.vb = [], [], [], []
+        last = len(self.cin) - 1
+        for l, (ci, co) in enumerate(zip(self.cin, self.cout)):
             fan_in = 27 * ci
-            scale = (2.0 / fan_in) ** 0.5 if l < len(self.layers) - 1 else 0.1 * (1.0 / fan_in) ** 0.5
+            scale = (2.0 / fan_in) ** 0.5 if l < last else 0.1 * (1.0 / fan_in) ** 0.5
             w = (torch.randn(27, co, ci, generator=g) * scale).cuda()
             self.w.append(w)
-            self.b.append(torch.zeros(co, device="cuda"))
             self.wb.append(w.to(torch.bfloat16))
-            self.mw.append(torch.zeros_like(w))
-            self.vw.append(torch.zeros_like(w))
-            self.mb.append(torch.zeros(co, device="cuda"))
-            self.vb.append(torch.zeros(co, device="cuda"))
+            self.b.append(torch.zeros(co, device="cuda"))
+            for lst in (self.mw, self.vw):
+                lst.append(torch.zeros_like(w))
+            for lst in (self.mb, self.vb):
+                lst.append(torch.zeros(co, device="cuda"))
         self.step = 0
-        self.out_scale = 1.0   # the model's correction is out_scale x the last layer's output
-
-    # -- forward / backward through the conv kernels ----------------------
-    def forward(self, n, feat):
-        """feat: CUDA BF16 [V][16]; returns the FP32 output [V][16] and keeps
-        the activations for backward."""
-        torch = self.torch
-        V = n[0] * n[1] * n[2]
-        self.acts = [feat]
-        x = feat
-        for l, (ci, co) in enumerate(self.layers):
-            last = l == len(self.layers) - 1
-            out = torch.empty(V, co, dtype=torch.float32 if last else torch.bfloat16, device="cuda")
-            check(lib().agb_conv3_forward(_cells(n), ci, co, _vp(x), _vp(self.wb[l]), _vp(self.b[l]), _vp(out),
-                                          int(last), int(not last), None))
-            if not last:
-                self.acts.append(out)
-            x = out
-        return x
-
-    def backward(self, n, dout):
-        """dout: FP32 [V][16] gradient of the loss w.r.t. the output; returns
-        the weight and bias gradients (FP32) of every layer."""
-        torch = self.torch
-        V = n[0] * n[1] * n[2]
-        gw, gb = [None] * len(self.layers), [None] * len(self.layers)
-        dy = dout.to(torch.bfloat16)
-        for l in range(len(self.layers) - 1, -1, -1):
-            ci, co = self.layers[l]
-            x = self.acts[l]
-            gw[l] = torch.zeros(27, co, ci, device="cuda")
-            gb[l] = torch.zeros(co, device="cuda")
-            check(lib().agb_conv3_wgrad(_cells(n), ci, co, _vp(x), _vp(dy), _vp(gw[l]), _vp(gb[l]), None))
-            if l == 0:
-                break
-            wt = torch.empty(27, ci, co, dtype=torch.bfloat16, device="cuda")
-            check(lib().agb_conv3_flip(ci, co, _vp(self.wb[l]), _vp(wt), None))
-            dx = torch.empty(V, ci, dtype=torch.bfloat16, device="cuda")
-            check(lib().agb_conv3_forward(_cells(n), co, ci, _vp(dy), _vp(wt), None, _vp(dx), 0, 0, None))
-            check(lib().agb_relu_backward(V * ci, _vp(x), _vp(dx), None))   # x = ReLU output of layer l-1
-            dy = dx
-        return gw, gb
-
-    def adam(self, gw, gb, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8):
-        self.step += 1
-        for l in range(len(self.layers)):
-            check(lib().agb_adam_step(self.w[l].numel(), _vp(self.w[l]), _vp(gw[l]), _vp(self.mw[l]),
-                                      _vp(self.vw[l]), _vp(self.wb[l]), lr, b1, b2, eps, self.step, None))
-            check(lib().agb_adam_step(self.b[l].numel(), _vp(self.b[l]), _vp(gb[l]), _vp(self.mb[l]),
-                                      _vp(self.vb[l]), None, lr, b1, b2, eps, self.step, None))
-
-    # -- export -----------------------------------------------------------
-    def export(self):
-        """(cin, cout, weights FP32 host, biases FP32 host) for agb_learned_create;
-        out_scale is folded into the last (linear) layer."""
-        cin = [c for c, _ in self.layers]
-        cout = [c for _, c in self.layers]
-        last = len(self.layers) - 1
-        w = np.concatenate([t.detach().cpu().numpy().reshape(-1) * (self.out_scale if l == last else 1.0)
-                            for l, t in enumerate(self.w)]).astype(np.float32)
-        b = np.concatenate([t.detach().cpu().numpy().reshape(-1) * (self.out_scale if l == last else 1.0)
-                            for l, t in enumerate(self.b)]).astype(np.float32)
-        return cin, cout, w, b
-
-    def state(self):
-        return {"layers": self.layers, "w": [t.cpu().numpy() for t in self.w], "b": [t.cpu().numpy() for t in self.b]}
-
-
-class LearnedHandle:
-    """agb_learned: the network as the solver uses it (BF16 weights on the device)."""
-
-    def __init__(self, net):
-        cin, cout, w, b = net.export()
+        w_h = np.concatenate([t.cpu().numpy().reshape(-1) for t in self.w]).astype(np.float32)
+        b_h = np.concatenate([t.cpu().numpy().reshape(-1) for t in self.b]).astype(np.float32)
         h = ctypes.c_void_p()
-        check(lib().agb_learned_create(len(cin), (ctypes.c_int * len(cin))(*cin), (ctypes.c_int * len(cout))(*cout),
-                                       w.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
-                                       b.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), ctypes.byref(h)))
+        check(lib().agb_unet_create(w_h.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                    b_h.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), ctypes.byref(h)))
         self.h = h
+        self.sync()
+        self._acts = None
 
     def close(self):
         if getattr(self, "h", None):
@@ -149,211 +96,256 @@ class LearnedHandle:
         except Exception:
             pass
 
+    def nparams(self):
+        return sum(t.numel() for t in self.w) + sum(t.numel() for t in self.b)
+
+    def sync(self):
+        """Hand the current BF16 weights and biases to the library's network."""
+        n = len(self.w)
+        wp = (ctypes.c_void_p * n)(*[t.data_ptr() for t in self.wb])
+        bp = (ctypes.c_void_p * n)(*[t.data_ptr() for t in self.b])
+        check(lib().agb_unet_set_weights(self.h, wp, bp, None))
+
+    # -- forward / backward --------------------------------------------------
+    def acts(self, g0):
+        """Activation buffers for a grid of g0 nodes (kept between calls)."""
+        torch = self.torch
+        key = tuple(g0)
+        if self._acts is None or self._acts[0] != key:
+            G = grids(g0)
+            bufs = [torch.empty(int(np.prod(G[self.alev[a]])) * self.ach[a], dtype=torch.bfloat16, device="cuda")
+                    for a in range(len(self.alev))]
+            out = torch.empty(int(np.prod(G[0])) * FEAT, dtype=torch.float32, device="cuda")
+            self._acts = (key, bufs, out)
+        return self._acts[1], self._acts[2]
+
+    def forward(self, g0, feat):
+        """feat: BF16 [V][16] on a grid of g0 nodes; returns the FP32 output
+        [V][16] (a view of a buffer reused by the next call)."""
+        bufs, out = self.acts(g0)
+        bufs[FEATS].copy_(feat.reshape(-1))
+        ptrs = (ctypes.c_void_p * len(bufs))(*[t.data_ptr() for t in bufs])
+        check(lib().agb_unet_forward(self.h, _i3(g0), ptrs, _vp(out), None))
+        return out.view(-1, FEAT)
+
+    def _dgrad(self, l, g, dy, dy_cs, dy_c0, out, out_cs, out_c0):
+        """out[:, out_c0 : out_c0 + cin_l] = data gradient of layer l at dy."""
+        torch = self.torch
+        L = lib()
+        ci, co = self.cin[l], self.cout[l]
+        wt = torch.empty(27 * ci * co, dtype=torch.bfloat16, device="cuda")
+        check(L.agb_conv3_flip(ci, co, _vp(self.wb[l]), _vp(wt), None))   # [27][ci][co]
+        c0 = 0
+        while c0 < ci:
+            w = min(64, ci - c0)
+            if w == 48 and ci - c0 > 48:
+                w = 32
+            wp = torch.empty(27 * co * w, dtype=torch.bfloat16, device="cuda")
+            check(L.agb_conv3_tc_pack(co, w, _vp(wt), ci, c0, _vp(wp), None))
+            check(L.agb_conv3_tc(_i3(g), co, w, _vp(dy), dy_cs, dy_c0, _vp(wp), None, _vp(out), out_cs, out_c0 + c0,
+                                 0, 0, None))
+            c0 += w
+
+    def _wgrad(self, l, g, x, x_cs, x_c0, dy, dy_cs, dy_c0, gw, gb):
+        check(lib().agb_conv3_wgrad0(_i3(g), self.cin[l], self.cout[l], _vp(x), x_cs, x_c0, _vp(dy), dy_cs, dy_c0,
+                                     _vp(gw[l]), _vp(gb[l]), None))
+
+    def _mask(self, V, C, y, y_cs, y_c0, m, m_cs, m_c0, b=None, b_cs=0, b_c0=0, beta=0.0):
+        check(lib().agb_axpby_mask(V, C, _vp(y), y_cs, y_c0, _vp(y), y_cs, y_c0, _vp(b), b_cs, b_c0, float(beta),
+                                   _vp(m), m_cs, m_c0, None))
+
+    def backward(self, g0, dout):
+        """dout: FP32 [V][16], the loss gradient at the output of the last
+        forward; returns the FP32 weight and bias gradients of every layer."""
+        torch = self.torch
+        L = lib()
+        G = grids(g0)
+        V = [int(np.prod(x)) for x in G]
+        a, _ = self.acts(g0)
+        gw = [torch.zeros(27, co, ci, device="cuda") for ci, co in zip(self.cin, self.cout)]
+        gb = [torch.zeros(co, device="cuda") for co in self.cout]
+
+        def buf(lev, c):
+            return torch.empty(V[lev] * c, dtype=torch.bfloat16, device="cuda")
+
+        dy = dout.reshape(-1).to(torch.bfloat16)
+        self._wgrad(10, G[0], a[H0], 16, 0, dy, 16, 0, gw, gb)
+        g_h0 = buf(0, 16)
+        self._dgrad(10, G[0], dy, 16, 0, g_h0, 16, 0)
+        self._mask(V[0], 16, g_h0, 16, 0, a[H0], 16, 0)
+        self._wgrad(9, G[0], a[F0], 16, 0, g_h0, 16, 0, gw, gb)
+        g_f0 = buf(0, 16)
+        self._dgrad(9, G[0], g_h0, 16, 0, g_f0, 16, 0)
+        self._mask(V[0], 16, g_f0, 16, 0, a[F0], 16, 0)
+        self._wgrad(8, G[0], a[CAT0], 48, 0, g_f0, 16, 0, gw, gb)
+        g_cat0 = buf(0, 48)
+        self._dgrad(8, G[0], g_f0, 16, 0, g_cat0, 48, 0)
+        g_e1 = buf(1, 32)
+        check(L.agb_grid_prolong_t(_i3(G[0]), _i3(G[1]), 32, _vp(g_cat0), 48, 0, _vp(g_e1), 32, 0, 0.0, 1.0, None))
+        self._mask(V[1], 32, g_e1, 32, 0, a[E1], 32, 0)
+        self._wgrad(7, G[1], a[D1], 32, 0, g_e1, 32, 0, gw, gb)
+        g_d1 = buf(1, 32)
+        self._dgrad(7, G[1], g_e1, 32, 0, g_d1, 32, 0)
+        self._mask(V[1], 32, g_d1, 32, 0, a[D1], 32, 0)
+        self._wgrad(6, G[1], a[CAT1], 96, 0, g_d1, 32, 0, gw, gb)
+        g_cat1 = buf(1, 96)
+        self._dgrad(6, G[1], g_d1, 32, 0, g_cat1, 96, 0)
+        g_c2 = buf(2, 64)
+        check(L.agb_grid_prolong_t(_i3(G[1]), _i3(G[2]), 64, _vp(g_cat1), 96, 0, _vp(g_c2), 64, 0, 0.0, 1.0, None))
+        self._mask(V[2], 64, g_c2, 64, 0, a[C2], 64, 0)
+        self._wgrad(5, G[2], a[C1], 64, 0, g_c2, 64, 0, gw, gb)
+        g_c1 = buf(2, 64)
+        self._dgrad(5, G[2], g_c2, 64, 0, g_c1, 64, 0)
+        self._mask(V[2], 64, g_c1, 64, 0, a[C1], 64, 0)
+        self._wgrad(4, G[2], a[P2], 32, 0, g_c1, 64, 0, gw, gb)
+        g_p2 = buf(2, 32)
+        self._dgrad(4, G[2], g_c1, 64, 0, g_p2, 32, 0)
+        # skip 1: its gradient from the concatenation plus (1/8) P of p2's
+        g_s1 = buf(1, 32)
+        check(L.agb_grid_prolong(_i3(G[1]), _i3(G[2]), 32, _vp(g_p2), 32, 0, _vp(g_s1), 32, 0, 0.0, 0.125, None))
+        self._mask(V[1], 32, g_s1, 32, 0, a[CAT1], 96, 64, b=g_cat1, b_cs=96, b_c0=64, beta=1.0)
+        self._wgrad(3, G[1], a[B1], 32, 0, g_s1, 32, 0, gw, gb)
+        g_b1 = buf(1, 32)
+        self._dgrad(3, G[1], g_s1, 32, 0, g_b1, 32, 0)
+        self._mask(V[1], 32, g_b1, 32, 0, a[B1], 32, 0)
+        self._wgrad(2, G[1], a[P1], 16, 0, g_b1, 32, 0, gw, gb)
+        g_p1 = buf(1, 16)
+        self._dgrad(2, G[1], g_b1, 32, 0, g_p1, 16, 0)
+        g_s0 = buf(0, 16)
+        check(L.agb_grid_prolong(_i3(G[0]), _i3(G[1]), 16, _vp(g_p1), 16, 0, _vp(g_s0), 16, 0, 0.0, 0.125, None))
+        self._mask(V[0], 16, g_s0, 16, 0, a[CAT0], 48, 32, b=g_cat0, b_cs=48, b_c0=32, beta=1.0)
+        self._wgrad(1, G[0], a[A1], 16, 0, g_s0, 16, 0, gw, gb)
+        g_a1 = buf(0, 16)
+        self._dgrad(1, G[0], g_s0, 16, 0, g_a1, 16, 0)
+        self._mask(V[0], 16, g_a1, 16, 0, a[A1], 16, 0)
+        self._wgrad(0, G[0], a[FEATS], 16, 0, g_a1, 16, 0, gw, gb)
+        return gw, gb
+
+    def adam(self, gw, gb, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8):
+        self.step += 1
+        L = lib()
+        for l in range(len(self.w)):
+            check(L.agb_adam_step(self.w[l].numel(), _vp(self.w[l]), _vp(gw[l]), _vp(self.mw[l]), _vp(self.vw[l]),
+                                  _vp(self.wb[l]), lr, b1, b2, eps, self.step, None))
+            check(L.agb_adam_step(self.b[l].numel(), _vp(self.b[l]), _vp(gb[l]), _vp(self.mb[l]), _vp(self.vb[l]),
+                                  None, lr, b1, b2, eps, self.step, None))
+        self.sync()
+
+    # -- use in a solve ------------------------------------------------------------
+    def attach(self, solver, min_gain=0.01, max_fail=2):
+        """Use the network in `solver` (a mixed-precision Linear with krylov > 0)."""
+        check(lib().agb_solver_set_learned(solver.h, self.h, float(min_gain), int(max_fail)))
+        solver._learned = self   # keep the network alive while the solver uses it
+
+    @staticmethod
+    def detach(solver):
+        check(lib().agb_solver_set_learned(solver.h, None, 0.01, 2))
+        solver._learned = None
+
+
+def learned_stats(solver):
+    """(directions tried, directions kept, network still in use) of the last solve."""
+    t, k, a = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    check(lib().agb_solver_learned_stats(solver.h, ctypes.byref(t), ctypes.byref(k), ctypes.byref(a)))
+    return t.value, k.value, bool(a.value)
+
+
+def features(op, r):
+    """BF16 features [V][16] of a residual r (reference layout, host or
+    device) of the operator's finest level, and the residual's RMS."""
+    import torch
+    V = op.nodes(0)
+    feat = torch.empty(V * FEAT, dtype=torch.bfloat16, device="cuda")
+    rms = ctypes.c_double()
+    pr, mem = _ptr(r)
+    check(lib().agb_unet_features(op.h, pr, mem, _vp(feat), ctypes.byref(rms)))
+    return feat.view(V, FEAT), rms.value
+
+
+def _channels_last(v, n):
+    """reference layout SoA (3, (n+1)^3) -> [V][3] FP32 (nodes = voxels)."""
+    import torch
+    t = v if hasattr(v, "data_ptr") else torch.from_numpy(np.ascontiguousarray(v)).cuda()
+    return t.reshape(3, -1).t().contiguous().float()
+
 
 # ---------------------------------------------------------------------------
 # training data and training
 # ---------------------------------------------------------------------------
-def unique_rms(v, n):
-    a = v.reshape(3, n + 1, n + 1, n + 1)[:, :n, :n, :n]
-    return float(np.sqrt(np.mean(a * a)))
-
-
-def features(n, r, ddw, scale):
-    """BF16 features [n^3][16] of a residual in the reference layout."""
-    import torch
-    rd = torch.from_numpy(np.ascontiguousarray(r)).cuda()
-    dd = ddw if hasattr(ddw, "data_ptr") else torch.from_numpy(np.ascontiguousarray(ddw)).cuda()
-    feat = torch.empty(n ** 3, FEAT, dtype=torch.bfloat16, device="cuda")
-    check(lib().agb_learned_features(_cells((n, n, n)), _vp(rd), _vp(dd), float(scale), _vp(feat), None))
-    return feat
-
-
-def training_pairs(n=64, count=8, seed=4242, rng_seed=1, contrast_max=100.0):
-    """Training samples on n^3 periodic RVEs: for each RVE and each of two
-    right-hand sides (its eigenstrain load and a random load), r1 = r -
-    A V(r) after one FP64 V-cycle and e1 = A^{-1} r - V(r).  Each sample is a
-    dict: op (the RVE's operator, kept for the residual loss), feat (BF16
-    network features of r1), rhat (r1 / s at the unique nodes, [V][3]),
-    target (e1 / (s h^2), [V][16]); s = RMS of r1."""
+def training_samples(count=64, n=64, seed=777, iterates=(1, 2, 3), log=None):
+    """Samples from multigrid solves of random cubic polycrystals (8-64
+    Voronoi grains of random orientation, the benchmark's moduli) under
+    TensionTest uniaxial_stress on n^3-cell boxes: for each problem and each
+    k in `iterates`, the residual r_k = b - A x_k of the k-th FP64 F-cycle
+    iterate from x = 0 and its error e_k = x - x_k against the converged
+    solution (FP32 cycles in FP64 refinement to 1e-10).  Each sample: feat
+    (BF16 [V][16] network features of r_k), target (e_k channels-last FP32
+    [V][3])."""
     import torch
     from . import microstructure as M
-    rng = np.random.default_rng(rng_seed)
-    pairs = []
+    from .elastic import TensionTest
+    rng = np.random.default_rng(seed)
+    N = (n + 1) ** 3
+    out = []
     for q in range(count):
-        _, ddw, F0 = M.rve_problem_device(q, seed=seed, edges=(n,), contrast_max=contrast_max)
-        op = Elastic([n] * 3, None, "isotropic", periodic=(1, 1, 1))
-        op.SetBC(_periodic_bc())
+        ng = int(rng.integers(8, 65))
+        ddw, _, _ = M.voronoi_cubic_device(n, ngrains=ng, seed=int(rng.integers(1, 2 ** 31)))
+        op = Elastic([n] * 3, None, "majorminor")
+        op.SetBC(TensionTest("uniaxial_stress", disp=0.01))
         op.SetModel(ddw)
-        N = (n + 1) ** 3
-        F0n = np.tile(np.asarray(F0).reshape(9), N)
-        b_eig = op.NewtonRHS(np.zeros(3 * N), np.zeros(3 * N), F0=F0n)
-        rnd = rng.standard_normal((3, n, n, n))
-        b_rnd = np.pad(rnd, ((0, 0), (0, 1), (0, 1), (0, 1)), mode="wrap").reshape(-1) * np.abs(b_eig).max()
-        for b in (b_eig, b_rnd):
-            b = b - _unique_mean(b, n)
-            one = Linear(op, fixed_iter=1, max_iter=1, max_fmg_iter=0)
-            x1 = np.zeros(3 * N)
-            one.solve(x1, b, 1e-30, 0.0, raise_on_fail=False)
-            one.Clear()
-            r1 = op.solutionResidual(0, x1, b)
-            r1 = r1 - _unique_mean(r1, n)
-            full = Linear(op, max_fmg_iter=0, precision=1)
-            xs = np.zeros(3 * N)
-            full.solve(xs, b, 1e-10, 0.0)
-            full.Clear()
-            e1 = xs - x1
-            e1 = e1 - _unique_mean(e1, n)
-            s = unique_rms(r1, n)
-            h2 = (1.0 / n) ** 2
-            feat = features(n, r1, ddw, s)
-            t = e1.reshape(3, n + 1, n + 1, n + 1)[:, :n, :n, :n].reshape(3, -1).T / (s * h2)
-            target = torch.zeros(n ** 3, FEAT, device="cuda")
-            target[:, :3] = torch.from_numpy(np.ascontiguousarray(t)).float().cuda()
-            rhat = _from_reference(torch.from_numpy(r1 / s).cuda(), n)
-            pairs.append({"op": op, "feat": feat, "target": target, "rhat": rhat})
-    return pairs
+        del ddw
+        zero = torch.zeros(3 * N, dtype=torch.float64, device="cuda")
+        b = op.BCInit(torch.zeros(3 * N, dtype=torch.float64, device="cuda"))
+        rhs = torch.empty(3 * N, dtype=torch.float64, device="cuda")
+        op.NewtonRHS(zero, b, out=rhs)
+        xs = torch.zeros(3 * N, dtype=torch.float64, device="cuda")
+        full = Linear(op, precision=1, krylov=8)
+        full.solve(xs, rhs, 1e-10, 0.0)
+        full.Clear()
+        for k in iterates:
+            s = Linear(op, fixed_iter=k, max_iter=k)
+            xk = torch.zeros(3 * N, dtype=torch.float64, device="cuda")
+            s.solve(xk, rhs, 1e-30, 0.0, raise_on_fail=False)
+            s.Clear()
+            rk = torch.empty(3 * N, dtype=torch.float64, device="cuda")
+            op.solutionResidual(0, xk, rhs, out=rk)
+            feat, _ = features(op, rk)
+            out.append({"feat": feat, "target": _channels_last(xs - xk, n)})
+        op.close()
+        if log and (q + 1) % max(1, count // 4) == 0:
+            log("training samples: %d of %d problems" % (q + 1, count))
+    return out
 
 
-def _unique_mean(v, n):
-    a = v.reshape(3, n + 1, n + 1, n + 1)
-    m = a[:, :n, :n, :n].reshape(3, -1).mean(axis=1)
-    return np.repeat(m, (n + 1) ** 3)
+def cosine_loss(out, target):
+    """1 - cos^2 between the correction out[:, 0:3] and the error, over all
+    nodes, and its gradient with respect to out (FP32 [V][16])."""
+    import torch
+    c = out[:, :3].double()
+    e = target.double()
+    ce = float((c * e).sum())
+    cc = float((c * c).sum())
+    ee = float((e * e).sum())
+    if cc <= 0 or ee <= 0:
+        return 1.0, torch.zeros_like(out)
+    loss = 1.0 - ce * ce / (cc * ee)
+    g = torch.zeros_like(out)
+    g[:, :3] = (-2.0 * ce / (cc * ee) * e + 2.0 * ce * ce / (cc * cc * ee) * c).float()
+    return loss, g
 
 
-def _periodic_bc():
-    from .elastic import Constant
-    return Constant()
-
-
-def train(net, pairs, n, steps=300, lr=2e-3):
-    """Adam on the mean squared error of output channels 0-2 against the
-    error targets; returns the loss history."""
-    V = n ** 3
-    net.out_scale = 1.0
+def train(net, samples, n, steps=1000, lr=1e-3, warmup=50, log=None):
+    """Adam on the cosine loss, one sample per step (cycling), the learning
+    rate ramped up over the first `warmup` steps.  Returns the loss history."""
+    g0 = (n + 1,) * 3
     hist = []
     for it in range(steps):
-        p = pairs[it % len(pairs)]
-        out = net.forward((n, n, n), p["feat"])
-        diff = out - p["target"]
-        diff[:, 3:] = 0.0
-        hist.append(float((diff[:, :3] ** 2).mean()))
-        dout = diff * (2.0 / (3 * V))
-        gw, gb = net.backward((n, n, n), dout)
-        net.adam(gw, gb, lr=lr)
+        smp = samples[it % len(samples)]
+        out = net.forward(g0, smp["feat"])
+        loss, dout = cosine_loss(out, smp["target"])
+        hist.append(loss)
+        gw, gb = net.backward(g0, dout)
+        net.adam(gw, gb, lr=lr * min(1.0, (it + 1) / float(warmup)))
+        if log and (it + 1) % max(1, steps // 5) == 0:
+            log("step %d: mean loss over the last %d steps %.4f" % (it + 1, min(it + 1, 50), float(np.mean(hist[-50:]))))
     return hist
-
-
-def _to_reference(u_cl, n):
-    """[V][3] channels-last (V = x + n (y + n z)) -> reference layout SoA over
-    (n+1)^3 nodes with the periodic duplicates, float64."""
-    import torch
-    a = u_cl.reshape(n, n, n, 3).permute(3, 0, 1, 2)
-    a = torch.cat([a, a[:, :1]], dim=1)
-    a = torch.cat([a, a[:, :, :1]], dim=2)
-    a = torch.cat([a, a[:, :, :, :1]], dim=3)
-    return a.reshape(-1).double().contiguous()
-
-
-def _from_reference(v, n):
-    """reference layout (3, n+1, n+1, n+1) -> [V][3] at the unique nodes."""
-    a = v.reshape(3, n + 1, n + 1, n + 1)[:, :n, :n, :n]
-    return a.permute(1, 2, 3, 0).reshape(-1, 3)
-
-
-def _highpass(op, v):
-    """(I - P R) v on the finest level: the part of v that the next coarser
-    level cannot represent (R full weighting, P trilinear prolongation;
-    R = P^T / 8, so the filter is symmetric)."""
-    import torch
-    crse = torch.zeros(op.nodes(1) * 3, dtype=torch.float64, device="cuda")
-    op.restriction(1, v, crse)
-    smooth = torch.zeros_like(v)
-    op.interpolation(0, smooth, crse)
-    return v - smooth
-
-
-def train_highpass(net, pairs, n, steps=300, lr=5e-5, warmup=50):
-    """Adam on the high-frequency part of the correction's error, in units
-    of s: per sample, loss_k = mean |H (c - e1 / (s h^2))|^2 / w_k over the
-    unique nodes, c = sigma x the network output, H = I - P R, w_k = mean
-    |H t_k|^2 (each sample weighs the same), sigma = RMS of H of the targets
-    over the samples (so the output the loss asks for is of order one;
-    sigma becomes net.out_scale).  One Adam step per pass over all samples
-    (gradients summed), the learning rate ramped up over the first `warmup`
-    steps (Adam's first steps move every weight by the full rate at once).  A local correction can only match the part of the
-    remaining error that the coarse levels do not represent, and that part
-    is what leaves the residual rough.  The gradient is exact (H is
-    symmetric).  Returns the history of the mean loss."""
-    import torch
-    V = n ** 3
-    wk = []
-    for p in pairs:
-        if "t_ref" not in p:
-            p["t_ref"] = _to_reference(p["target"][:, :3], n)
-        wk.append(float((_from_reference(_highpass(p["op"], p["t_ref"]), n) ** 2).mean()))
-    sigma = float(np.sqrt(np.mean(wk))) or 1.0
-    net.out_scale = sigma
-    hist = []
-    for it in range(steps):
-        gsum_w, gsum_b, total = None, None, 0.0
-        for k, p in enumerate(pairs):
-            out = net.forward((n, n, n), p["feat"])
-            d = _to_reference(out[:, :3].double() * sigma, n) - p["t_ref"]
-            hu = _from_reference(_highpass(p["op"], d), n)
-            total += float((hu ** 2).mean()) / wk[k]
-            g = _from_reference(_highpass(p["op"], _to_reference(hu, n)), n) * (2.0 * sigma / (3 * V * wk[k]))
-            dout = torch.zeros_like(out)
-            dout[:, :3] = g.float()
-            gw, gb = net.backward((n, n, n), dout)
-            if gsum_w is None:
-                gsum_w, gsum_b = gw, gb
-            else:
-                for l in range(len(gw)):
-                    gsum_w[l] += gw[l]
-                    gsum_b[l] += gb[l]
-        hist.append(total / len(pairs))
-        net.adam(gsum_w, gsum_b, lr=lr * min(1.0, (it + 1) / float(warmup)))
-    return hist
-
-
-# ---------------------------------------------------------------------------
-# solve
-# ---------------------------------------------------------------------------
-class LearnedSolver:
-    """agb_learned_solve on an operator: GCR with V-cycle (+ learned) directions."""
-
-    def __init__(self, op, net=None, restart=8, **params):
-        params.setdefault("max_iter", 200)
-        self.params = default_params(**params)
-        h = ctypes.c_void_p()
-        check(lib().agb_solver_create(op.h, ctypes.byref(self.params), ctypes.byref(h)))
-        self.h = h
-        self.op = op
-        self.handle = LearnedHandle(net) if net is not None else None
-        self.restart = restart
-        self.report = None
-
-    def solve(self, sol, rhs, tol_rel=1e-8, tol_abs=0.0, raise_on_fail=True):
-        rep = _lib.AgbSolveReport()
-        ps, mem = _ptr(sol)
-        pr, _ = _ptr(rhs)
-        st = lib().agb_learned_solve(self.h, self.handle.h if self.handle else None, ps, pr, float(tol_rel),
-                                     float(tol_abs), int(self.restart), mem, ctypes.byref(rep))
-        self.report = rep
-        if st != _lib.AGB_OK and raise_on_fail:
-            check(st)
-        return rep.res_final
-
-    def close(self):
-        if getattr(self, "h", None):
-            lib().agb_solver_destroy(self.h)
-            self.h = None
-        if self.handle:
-            self.handle.close()
-            self.handle = None
-
-    def __del__(self):
-        try:
-            self.close()
-        except Exception:
-            pass

@@ -265,30 +265,6 @@ agb_status agb_gen_ellipsoids(const int n_cells[3], int ninc, const double* incl
 agb_status agb_gen_sphere(const int n_cells[3], double radius, double lam_m, double mu_m, double lam_i, double mu_i,
                           double eig, double* ddw, double* F0, int mem, void* stream);
 
-/* 3x3x3 convolutions of the learned preconditioner (no reference
- * counterpart).  Fields are channels-last BF16 [voxel][C] over a fully
- * periodic box of n[0] x n[1] x n[2] voxels (voxel = x + n0 (y + n1 z); edges
- * multiples of 16, 4 and 2), C a multiple of 16 (unused channels zero).
- * Weights are BF16 [27][Cout][Cin], tap = (dx+1) + 3 (dy+1) + 9 (dz+1).
- * Device pointers; work is queued on `stream` and not waited for.
- *   forward: out[v][co] = act(bias[co] + sum_tap sum_ci in[v+off(tap)][ci] w[tap][co][ci]),
- *            out FP32 (out_f32) or BF16, act = ReLU if relu.
- *   wgrad:   dw[tap][co][ci] += sum_v dy[v][co] in[v+off(tap)][ci] (FP32,
- *            accumulated), db[co] += sum_v dy[v][co] (db may be NULL).
- *   flip:    wt[26-tap][ci][co] = w[tap][co][ci]; the data gradient of a layer
- *            is agb_conv3_forward(dy, wt).
- *   relu_backward: dy[e] = 0 where y[e] <= 0 (BF16, count elements).
- *   adam_step: Adam on FP32 weights w with gradient g and moments m, v; the
- *            BF16 copy w_bf16 (may be NULL) is refreshed. */
-agb_status agb_conv3_forward(const int n[3], int cin, int cout, const void* in, const void* w, const float* bias,
-                             void* out, int out_f32, int relu, void* stream);
-agb_status agb_conv3_wgrad(const int n[3], int cin, int cout, const void* in, const void* dy, float* dw, float* db,
-                           void* stream);
-agb_status agb_conv3_flip(int cin, int cout, const void* w, void* wt, void* stream);
-agb_status agb_relu_backward(long long count, const void* y, void* dy, void* stream);
-agb_status agb_adam_step(long long count, float* w, const float* g, float* m, float* v, void* w_bf16, float lr,
-                         float beta1, float beta2, float eps, int step, void* stream);
-
 /* 3x3x3 convolution on the fifth-generation tensor cores (tcgen05.mma with
  * the accumulator in tensor memory, halo lines brought by TMA), zero padding
  * outside the box, any box size; no reference counterpart.  Fields are
@@ -297,45 +273,81 @@ agb_status agb_adam_step(long long count, float* w, const float* g, float* m, fl
  * cout) (slice starts multiples of 8), so a concatenation of skip inputs is
  * one buffer.  cin a multiple of 16, cout 16, 32, 48 or 64.  wp holds the
  * weights packed by agb_conv3_tc_pack from [27][cout][cin] BF16 (27 cin cout
- * elements); bias (FP32, cout) may be NULL; out FP32 when out_f32; ReLU when
+ * elements: rows w_co0 .. w_co0 + cout of a [27][w_cout][cin] array, so a wide
+ * layer runs as several convolutions); bias (FP32, cout) may be NULL; out FP32 when out_f32; ReLU when
  * relu.  Device pointers, 16-byte aligned; queued on `stream`.
  * agb_conv3_tc_error reports (and clears) a bounded wait of the kernel that
  * ran out since the last call. */
-agb_status agb_conv3_tc_pack(int cin, int cout, const void* w, void* wp, void* stream);
+agb_status agb_conv3_tc_pack(int cin, int cout, const void* w, int w_cout, int w_co0, void* wp, void* stream);
 agb_status agb_conv3_tc(const int n[3], int cin, int cout, const void* in, int in_cs, int in_c0, const void* wp,
                         const float* bias, void* out, int out_cs, int out_c0, int out_f32, int relu, void* stream);
 agb_status agb_conv3_tc_error(int* flag);
 
-/* Learned correction inside a flexible GCR solve (no reference counterpart).
- * The network is a stack of agb_conv3 layers (channels 16/32/48; the first
- * takes 16 channels, the last gives 16; hidden layers ReLU, the last linear)
- * applied to the finest level of a fully periodic isotropic box whose edges
- * are multiples of 16, 4 and 2: features r/s (3), log(lambda)/4, log(mu)/4, zeros
- * (s = RMS of r); output channels 0-2 times s h^2 are a displacement
- * correction.  Weights are FP32 on the host, [27][cout][cin] per layer,
- * stored as BF16 on the device. */
+/* Learned correction (no reference counterpart): a three-level
+ * convolutional encoder-decoder (U-Net, channels 16/32/64, 3x3x3
+ * convolutions on the tensor cores with zero padding, skip connections,
+ * full-weighting down and trilinear up between nodal grids of g, (g-1)/2+1
+ * and (g-1)/4+1 nodes) that maps the features of a residual -- r / s (s its
+ * RMS), half logs of the axial and shear moduli, a boundary flag -- to a
+ * displacement correction (output channels 0-2 times s h^2).  Set on a
+ * mixed-precision solver with krylov > 0, every inner GCR iteration adds,
+ * after the multigrid direction, the network's direction on the residual the
+ * cycle left; it is kept if it removes at least min_gain of the weighted
+ * residual norm squared, and after max_fail rejections in a row -- or a
+ * refinement step whose FP64 residual stalls -- the solve goes on with the
+ * multigrid directions alone.  Boxes: no periodic direction, edges divisible
+ * by 4.
+ *   agb_unet_layers / agb_unet_acts: the topology (per layer cin, cout, grid
+ *     level; per forward activation its grid level and channels).
+ *   agb_unet_create: weights [27][cout][cin] FP32 per layer, concatenated,
+ *     and biases (cout per layer).
+ *   agb_unet_set_weights: replace the weights from device BF16 arrays and
+ *     FP32 biases, one pointer per layer (training).
+ *   agb_unet_forward: the forward pass on a grid of g0 nodes (edges 4 m + 1),
+ *     acts[0] the features, acts[1..] the other activations (caller-owned
+ *     device buffers, kept for the backward pass), out FP32 [voxel][16].
+ *   agb_unet_features: the features of a residual (reference layout, host
+ *     or device per mem) of an operator's finest level, and its RMS.
+ *   agb_solver_set_learned / agb_solver_learned_stats: attach a network
+ *     (NULL detaches) and read the last solve's counts of learned directions
+ *     tried and kept, and whether the network was still in use at its end. */
+#define AGB_UNET_LAYERS 11
+#define AGB_UNET_ACTS 13
 typedef struct agb_learned_s* agb_learned;
-agb_status agb_learned_create(int nlayers, const int* cin, const int* cout, const float* weights, const float* biases,
-                              agb_learned* out);
+agb_status agb_unet_layers(int* cin, int* cout, int* level);
+agb_status agb_unet_acts(int* level, int* channels);
+agb_status agb_unet_create(const float* weights, const float* biases, agb_learned* out);
+agb_status agb_unet_set_weights(agb_learned net, const void* const* w_bf16, const float* const* biases, void* stream);
+agb_status agb_unet_forward(agb_learned net, const int g0[3], void* const* acts, float* out, void* stream);
+agb_status agb_unet_features(agb_op op, const double* r, int mem, void* feat, double* rms);
 agb_status agb_learned_destroy(agb_learned net);
-/* Network features of a residual in the reference layout (SoA over (n+1)^3
- * nodes, periodic duplicates ignored) and isotropic AoS moduli, divided by
- * `scale`: BF16 [n0 n1 n2][16], device pointers, queued on `stream`. */
-agb_status agb_learned_features(const int n_cells[3], const double* r, const double* ddw, double scale, void* feat,
-                                void* stream);
-/* Flexible GCR (restart after `restart` stored directions) on the solver's
- * operator, to ||b - A x||_inf <= max(tol_abs, tol_rel max(||b||, ||r0||)).
- * Each iteration adds the direction V(r) (one FP32 V-cycle of the solver's
- * multigrid settings) and, with a network, the learned direction N(r) on the
- * residual that step left; GCR minimises the residual over all stored
- * directions, so a learned direction that does not help costs its work but
- * not convergence, and the V-cycle directions carry the solve (the
- * fallback).  net = NULL gives V-cycle GCR, the ablation baseline.  Fully
- * periodic boxes use the zero-mean projection of agb_solve.
- * report->iterations counts V-cycle directions; report->refinements counts
- * learned directions that reduced ||r||_2 by less than 1 %. */
-agb_status agb_learned_solve(agb_solver s, agb_learned net, double* sol, const double* rhs, double tol_rel,
-                             double tol_abs, int restart, int mem, agb_solve_report* report);
+agb_status agb_solver_set_learned(agb_solver s, agb_learned net, double min_gain, int max_fail);
+agb_status agb_solver_learned_stats(agb_solver s, int* tried, int* kept, int* active);
+
+/* Training kernels of the learned correction, channels-last BF16 fields over
+ * nodal grids g (voxel = x + g0 (y + g1 z)), channel slices [c0, c0 + C) of
+ * buffers with channel stride cs; device pointers, queued on `stream`.
+ *   wgrad0: dw[tap][co][ci] += sum_v dy[v][co] x[v + off(tap)][ci], zero
+ *     padding (FP32, accumulated); db[co] += sum_v dy[v][co] (db may be NULL).
+ *   flip: wt[26 - tap][ci][co] = w[tap][co][ci]; the data gradient of a layer
+ *     is the forward convolution of dy with wt.
+ *   grid_prolong: fine = beta fine + s P coarse (trilinear, fine = 2 (coarse
+ *     - 1) + 1 nodes); grid_prolong_t: coarse = beta coarse + s P^T fine.
+ *   axpby_mask: y = (a + beta b) where m > 0, else 0 (b, m may be NULL).
+ *   adam_step: Adam on FP32 weights w with gradient g and moments m, v; the
+ *     BF16 copy w_bf16 (may be NULL) is refreshed. */
+agb_status agb_conv3_wgrad0(const int g[3], int cin, int cout, const void* x, int x_cs, int x_c0, const void* dy,
+                            int dy_cs, int dy_c0, float* dw, float* db, void* stream);
+agb_status agb_conv3_flip(int cin, int cout, const void* w, void* wt, void* stream);
+agb_status agb_grid_prolong(const int gf[3], const int gc[3], int C, const void* crs, int c_cs, int c_c0, void* fine,
+                            int f_cs, int f_c0, float beta, float s, void* stream);
+agb_status agb_grid_prolong_t(const int gf[3], const int gc[3], int C, const void* fine, int f_cs, int f_c0, void* crs,
+                              int c_cs, int c_c0, float beta, float s, void* stream);
+agb_status agb_axpby_mask(long long nvox, int C, void* y, int y_cs, int y_c0, const void* a, int a_cs, int a_c0,
+                          const void* b, int b_cs, int b_c0, float beta, const void* m, int m_cs, int m_c0,
+                          void* stream);
+agb_status agb_adam_step(long long count, float* w, const float* g, float* m, float* v, void* w_bf16, float lr,
+                         float beta1, float beta2, float eps, int step, void* stream);
 
 /* Allocation-free coarsest-level solve.  No counterpart in the reference: it
  * exists for callers that may not allocate device memory when they need a

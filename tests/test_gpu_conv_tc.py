@@ -54,7 +54,7 @@ def test_conv3_tc_matches_torch(gpu_lib, n, cin, cout, out_f32, relu):
     out = torch.full((V, out_cs), 7.0, dtype=odt).cuda()
     d_in, d_w, d_b = xin.cuda(), w.cuda(), b.cuda()
     d_wp = torch.empty(27 * cout * cin, dtype=torch.bfloat16, device="cuda")
-    check(L.agb_conv3_tc_pack(cin, cout, vp(d_w), vp(d_wp), None))
+    check(L.agb_conv3_tc_pack(cin, cout, vp(d_w), cout, 0, vp(d_wp), None))
     for rep in range(2):
         check(L.agb_conv3_tc((ctypes.c_int * 3)(*n), cin, cout, vp(d_in), in_cs, in_c0, vp(d_wp), vp(d_b), vp(out),
                              out_cs, out_c0, int(out_f32), int(relu), None))

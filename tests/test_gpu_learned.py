@@ -1,128 +1,152 @@
-"""GPU: the learned correction (alamo_gb300.learned, agb_learned_*).
+"""GPU: the learned correction (the library's U-Net and its training kernels).
 
-* The network's gradients through the conv kernels against torch's CPU
-  autograd in FP64 on the same BF16-rounded weights, inputs and activations.
-* GCR with V-cycle directions against the oracle's solution of the same
-  periodic RVE.
-* Training reduces the loss, and the learned GCR converges to the same
-  solution; the ablation (same problem, same GCR, without the network) is
-  reported side by side.
+* The forward pass (agb_unet_forward) and the weight gradients of the
+  backward pass (chained from agb_conv3_wgrad0, flipped-weight data gradients
+  on the tensor cores, grid transfers and ReLU masks) against torch's FP64
+  CPU autograd on the same graph: zero-padded 3x3x3 convolutions, P^T / 8
+  down (a stride-2 convolution with the [1/2, 1, 1/2]^3 stencil) and P up
+  (its transpose), skip concatenations, every stored activation rounded to
+  BF16 as the kernels store it.
+* A few Adam steps on multigrid samples lower the loss.
+* A mixed-precision solve with the network attached converges to the
+  oracle's solution, and the network's directions are tried.
 """
-import sys
-
 import numpy as np
 import pytest
 
 import oracle as O
+from helpers import rel_err
 
 pytestmark = pytest.mark.gpu
 
 torch = pytest.importorskip("torch")
 
 
-def ref_forward(x_cl, ws, bs, n, layers):
-    """FP64 CPU forward with the kernels' BF16 rounding of hidden activations."""
+def torch_unet(net, feat, g0):
+    """The U-Net restated in torch FP64 from the network's BF16 weights; returns
+    (output [V][16], list of the weight tensors (leaves with gradients))."""
     F = torch.nn.functional
-    x = x_cl.double().reshape(n[2], n[1], n[0], -1).permute(3, 0, 1, 2).unsqueeze(0)
-    for l, (ci, co) in enumerate(layers):
-        w = ws[l].double().reshape(3, 3, 3, co, ci).permute(3, 4, 0, 1, 2)
-        x = F.conv3d(F.pad(x, (1, 1, 1, 1, 1, 1), mode="circular"), w, bs[l].double())
-        if l < len(layers) - 1:
-            x = torch.relu(x).to(torch.bfloat16).double()
-    return x[0].permute(1, 2, 3, 0).reshape(-1, layers[-1][1])
+    Wt, Bt = [], []
+    for l in range(len(net.w)):
+        ci, co = net.cin[l], net.cout[l]
+        w = net.wb[l].double().cpu().reshape(3, 3, 3, co, ci).permute(3, 4, 0, 1, 2).contiguous().requires_grad_(True)
+        b = net.b[l].double().cpu().clone().requires_grad_(True)
+        Wt.append(w)
+        Bt.append(b)
+    k1 = torch.tensor([0.5, 1.0, 0.5], dtype=torch.float64)
+    K = (k1[:, None, None] * k1[None, :, None] * k1[None, None, :])
+
+    def bf(x):   # stored as BF16 (straight-through for the gradient)
+        return x + (x.to(torch.bfloat16).double() - x).detach()
+
+    def conv(l, x, relu=True):
+        y = F.conv3d(x, Wt[l], Bt[l], padding=1)
+        return bf(torch.relu(y)) if relu else y
+
+    def down(x):
+        C = x.shape[1]
+        return bf(F.conv3d(x, K.expand(C, 1, 3, 3, 3), stride=2, padding=1, groups=C) / 8.0)
+
+    def up(x):
+        C = x.shape[1]
+        return bf(F.conv_transpose3d(x, K.expand(C, 1, 3, 3, 3), stride=2, padding=1, groups=C))
+
+    x = feat.double().cpu().reshape(g0[2], g0[1], g0[0], 16).permute(3, 0, 1, 2).unsqueeze(0)
+    a1 = conv(0, x)
+    s0 = conv(1, a1)
+    b1 = conv(2, down(s0))
+    s1 = conv(3, b1)
+    c2 = conv(5, conv(4, down(s1)))
+    d1 = conv(6, torch.cat([up(c2), s1], dim=1))
+    e1 = conv(7, d1)
+    f0 = conv(8, torch.cat([up(e1), s0], dim=1))
+    out = conv(10, conv(9, f0), relu=False)
+    return out[0].permute(1, 2, 3, 0).reshape(-1, 16), Wt, Bt
 
 
-def test_network_gradients_match_cpu_autograd(gpu_lib):
-    from alamo_gb300.learned import ConvNet
-    layers = ((16, 32), (32, 16), (16, 16))
-    n = (16, 4, 4)
-    V = n[0] * n[1] * n[2]
-    net = ConvNet(layers, seed=3)
-    for l in range(len(layers)):
-        net.b[l].normal_(0, 0.05)
-    g = torch.Generator().manual_seed(11)
-    feat = (torch.randn(V, 16, generator=g)).to(torch.bfloat16)
-    target = torch.randn(V, 16, generator=g) * 0.1
-    out = net.forward(n, feat.cuda())
-    dout = (out - target.cuda()) * (2.0 / out.numel())
-    gw, gb = net.backward(n, dout)
-    # reference: the same loss in FP64 through torch autograd on the CPU
-    ws = [w.detach().cpu().to(torch.bfloat16).double().requires_grad_(True) for w in net.w]
-    bs = [b.detach().cpu().double().requires_grad_(True) for b in net.b]
-    y = ref_forward(feat, ws, bs, n, layers)
-    loss = ((y - target.double()) ** 2).mean()
-    loss.backward()
-    assert (out.cpu().double() - y.detach()).abs().max() <= 1e-2 * y.detach().abs().max()
-    for l in range(len(layers)):
-        for got, ref in ((gw[l], ws[l].grad), (gb[l], bs[l].grad)):
-            err = (got.cpu().double() - ref).abs().max().item() / ref.abs().max().item()
-            assert err < 3e-2, (l, err)
-
-
-def rve(q, n, seed=4242):
+def make_net_and_features(n=16, seed=3):
+    from alamo_gb300 import Elastic
     from alamo_gb300 import microstructure as M
-    from alamo_gb300.elastic import Constant, Elastic
-    _, ddw, F0 = M.rve_problem(q, seed=seed, edges=(n,))
-    op = Elastic([n] * 3, None, "isotropic", periodic=(1, 1, 1))
-    op.SetBC(Constant())
+    from alamo_gb300.elastic import TensionTest
+    from alamo_gb300.learned import UNet, features
+    ddw, _, _ = M.voronoi_cubic(n, ngrains=5, seed=seed)
+    op = Elastic([n] * 3, None, "majorminor")
+    op.SetBC(TensionTest("uniaxial_stress", disp=0.01))
     op.SetModel(ddw)
-    N = (n + 1) ** 3
-    rhs = op.NewtonRHS(np.zeros(3 * N), np.zeros(3 * N), F0=np.tile(np.asarray(F0).reshape(9), N))
-    return op, ddw, rhs
+    r = np.random.default_rng(seed).standard_normal(3 * op.nodes(0))
+    feat, rms = features(op, r)
+    net = UNet(seed=seed)
+    return op, net, feat, rms, r, ddw
 
 
-def zero_mean(u, n):
-    a = u.reshape(3, n + 1, n + 1, n + 1)
-    m = a[:, :n, :n, :n].reshape(3, -1).mean(axis=1)
-    return (a - m[:, None, None, None]).reshape(-1)
-
-
-def test_vcycle_gcr_matches_oracle(gpu_lib):
-    from alamo_gb300.learned import LearnedSolver
-    n = 32
-    op, ddw, rhs = rve(2, n)
-    s = LearnedSolver(op, None, restart=8)
-    x = np.zeros_like(rhs)
-    s.solve(x, rhs, 1e-9, 0.0)
-    assert s.report.status == 0
-    g = O.make_grid([n] * 3, sym=O.ISO, periodic=(1, 1, 1))
-    xo, rep = O.solve(g, ddw, rhs, tol_rel=1e-10, tol_abs=0.0, params=O.default_params(max_fmg_iter=0))
-    assert rep.status == 0
-    err = np.abs(zero_mean(x, n) - xo).max() / np.abs(xo).max()
-    assert err < 1e-6, err
-    s.close()
+def test_unet_forward_and_gradients_match_torch(gpu_lib):
+    from alamo_gb300.learned import cosine_loss
+    op, net, feat, rms, r, ddw = make_net_and_features()
+    g0 = (17, 17, 17)
+    assert net.nparams() == 366336 + sum(net.cout)
+    # features: r / rms in channels 0-2, half logs of the moduli, the boundary flag
+    f = feat.double().cpu().numpy()
+    assert np.allclose(f[:, 0], r[:17 ** 3] / rms, rtol=1e-2, atol=1e-2)
+    assert f[0, 9] == 1.0 and f[17 * 17 * 8 + 17 * 8 + 8, 9] == 0.0
+    c = ddw.reshape(-1, 21)
+    assert np.allclose(f[:, 3], 0.5 * np.log(c[:, 0]), rtol=1e-2, atol=1e-2)
+    out = net.forward(g0, feat).clone()
+    ref, Wt, Bt = torch_unet(net, feat, g0)
+    e = float((out.double().cpu() - ref.detach()).abs().max() / ref.detach().abs().max())
+    assert e < 2e-2, e
+    target = torch.randn(17 ** 3, 3, generator=torch.Generator().manual_seed(5)).cuda()
+    loss, dout = cosine_loss(out, target)
+    gw, gb = net.backward(g0, dout)
+    lt, _ = cosine_loss(ref, target.cpu())
+    c_ = ref[:, :3]
+    t_ = target.double().cpu()
+    ce = (c_ * t_).sum()
+    L = 1.0 - ce * ce / ((c_ * c_).sum() * (t_ * t_).sum())
+    L.backward()
+    assert abs(float(L) - loss) < 1e-2
+    for l in range(len(Wt)):
+        gref = Wt[l].grad.permute(2, 3, 4, 0, 1).reshape(27, net.cout[l], net.cin[l])
+        eg = rel_err(gw[l].double().cpu().numpy(), gref.numpy())
+        eb = rel_err(gb[l].double().cpu().numpy(), Bt[l].grad.numpy())
+        print("layer %d: weight gradient rel err %.2e, bias %.2e" % (l, eg, eb))
+        assert eg < 5e-2 and eb < 5e-2, (l, eg, eb)
     op.close()
 
 
-def test_training_and_learned_gcr(gpu_lib, capsys):
-    from alamo_gb300.learned import ConvNet, LearnedSolver, train, train_highpass, training_pairs
+def test_training_lowers_the_loss(gpu_lib):
+    from alamo_gb300.learned import UNet, train, training_samples
+    smp = training_samples(count=2, n=16, seed=11)
+    net = UNet(seed=1)
+    hist = train(net, smp, 16, steps=60, lr=1e-3, warmup=10)
+    assert np.mean(hist[-10:]) < np.mean(hist[:10]), (hist[:10], hist[-10:])
+
+
+def test_learned_mixed_solve_matches_oracle(gpu_lib):
+    from alamo_gb300 import Elastic, Linear
+    from alamo_gb300 import microstructure as M
+    from alamo_gb300.elastic import TensionTest
+    from alamo_gb300.learned import UNet, learned_stats
+    from helpers import tension_bc_arrays
     n = 32
-    pairs = training_pairs(n=n, count=2, seed=777)
-    net_e = ConvNet(seed=2)
-    hist = train(net_e, pairs, n, steps=40, lr=2e-3)
-    assert np.mean(hist[-4:]) < np.mean(hist[:4]), (hist[:4], hist[-4:])
-    net = ConvNet(seed=1)
-    hist = train_highpass(net, pairs, n, steps=150, lr=5e-5)
-    assert np.mean(hist[-4:]) < 0.8 * hist[0], (hist[:4], hist[-4:])
-    with capsys.disabled():
-        sys.stderr.write("\nhigh-pass loss: first %.4g last %.4g\n" % (np.mean(hist[:4]), np.mean(hist[-4:])))
-    op, ddw, rhs = rve(5, n)
-    base = LearnedSolver(op, None, restart=16)
-    xb = np.zeros_like(rhs)
-    base.solve(xb, rhs, 1e-8, 0.0)
-    lrn = LearnedSolver(op, net, restart=16)
-    xl = np.zeros_like(rhs)
-    lrn.solve(xl, rhs, 1e-8, 0.0)
-    assert base.report.status == 0 and lrn.report.status == 0
-    err = np.abs(xl - xb).max() / np.abs(xb).max()
-    assert err < 1e-6, err
-    with capsys.disabled():
-        sys.stderr.write("\nablation (32^3 RVE, GCR restart 16): V-cycle %d steps %.1f ms; V-cycle+learned %d steps "
-                         "(%d fallbacks) %.1f ms\n" % (base.report.iterations, base.report.solve_ms,
-                                                       lrn.report.iterations, lrn.report.refinements,
-                                                       lrn.report.solve_ms))
-    # GCR minimises over every stored direction: the learned ones cannot slow it
-    assert lrn.report.iterations <= base.report.iterations + 1
-    base.close()
-    lrn.close()
+    ddw, _, _ = M.voronoi_cubic(n, ngrains=12, seed=21)
+    bt, bv = tension_bc_arrays(0.01)
+    g = O.make_grid([n] * 3, sym=O.MAJORMINOR, bc_type=bt, bc_val=bv)
+    N = O.nodes(g)
+    b = O.bc_init(g, np.zeros(3 * N))
+    rhs = O.newton_rhs(g, ddw, None, np.zeros(3 * N), b)
+    xo, _ = O.solve(g, ddw, rhs, tol_rel=1e-8, tol_abs=0.0)
+    op = Elastic([n] * 3, None, "majorminor")
+    op.SetBC(TensionTest("uniaxial_stress", disp=0.01))
+    op.SetModel(ddw)
+    net = UNet(seed=2)
+    s = Linear(op, precision=1, krylov=8)
+    net.attach(s, min_gain=0.0, max_fail=1000)   # keep every direction: exercises the GCR with them
+    x = np.zeros(3 * N)
+    s.solve(x, rhs, 1e-8, 0.0)
+    tried, kept, _ = learned_stats(s)
+    assert s.report.status == 0 and tried > 0 and kept > 0
+    r = O.residual(g, ddw, x, rhs)
+    assert np.abs(r).max() <= 1e-8 * max(np.abs(rhs).max(), s.report.res0) * 1.000001
+    assert rel_err(x, xo) < 1e-6
+    s.Clear()
     op.close()
