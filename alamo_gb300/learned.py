@@ -17,6 +17,10 @@ and compute the loss.
     train            Adam on the cosine between the network's correction and
                      the error (GCR rescales every direction, so only the
                      direction matters)
+    operator_matrix  the finest-level operator of a small box as a sparse
+                     matrix, probed through the library's Fapply
+    train_gain       Adam on the quantity the solve's GCR keeps a direction
+                     for: the weighted cosine between A N(r) and r
 """
 import ctypes
 
@@ -348,4 +352,154 @@ def train(net, samples, n, steps=1000, lr=1e-3, warmup=50, log=None):
         net.adam(gw, gb, lr=lr * min(1.0, (it + 1) / float(warmup)))
         if log and (it + 1) % max(1, steps // 5) == 0:
             log("step %d: mean loss over the last %d steps %.4f" % (it + 1, min(it + 1, 50), float(np.mean(hist[-50:]))))
+    return hist
+
+
+# ---------------------------------------------------------------------------
+# training on the GCR gain
+# ---------------------------------------------------------------------------
+def operator_matrix(op):
+    """The FP64 finest-level operator A of `op` (no periodic direction) as a
+    torch sparse CSR matrix over the reference layout (3 components of the
+    (n+1)^3 nodes), probed with 81 applications of the library's Fapply:
+    every row's stencil lies in the 3 x 3 x 3 neighbourhood of its node, so
+    a probe that is 1 on component p of the nodes of one colour (i, j, k mod
+    3) returns, in each row, the one matrix entry of that row for that
+    colour and component."""
+    import torch
+    nx, ny, nz = [c + 1 for c in op.n]
+    N = nx * ny * nz
+    k, j, i = torch.meshgrid(torch.arange(nz, device="cuda"), torch.arange(ny, device="cuda"),
+                             torch.arange(nx, device="cuda"), indexing="ij")
+    i, j, k = i.reshape(-1), j.reshape(-1), k.reshape(-1)
+    rows, cols, vals = [], [], []
+    f = torch.empty(3 * N, dtype=torch.float64, device="cuda")
+    for cz in range(3):
+        for cy in range(3):
+            for cx in range(3):
+                colour = ((i % 3) == cx) & ((j % 3) == cy) & ((k % 3) == cz)
+                # the node of this colour in each node's neighbourhood
+                mi = i + ((cx - i) % 3 + 1) % 3 - 1
+                mj = j + ((cy - j) % 3 + 1) % 3 - 1
+                mk = k + ((cz - k) % 3 + 1) % 3 - 1
+                inside = (mi >= 0) & (mi < nx) & (mj >= 0) & (mj < ny) & (mk >= 0) & (mk < nz)
+                m = mi + nx * (mj + ny * mk)
+                for p in range(3):
+                    e = torch.zeros(3 * N, dtype=torch.float64, device="cuda")
+                    e[p * N:(p + 1) * N] = colour.double()
+                    op.Fapply(0, e, out=f)
+                    for c in range(3):
+                        v = f[c * N:(c + 1) * N]
+                        keep = inside & (v != 0)
+                        rows.append((c * N + torch.arange(N, device="cuda"))[keep])
+                        cols.append((p * N + m)[keep])
+                        vals.append(v[keep])
+    r = torch.cat(rows)
+    c = torch.cat(cols)
+    v = torch.cat(vals)
+    A = torch.sparse_coo_tensor(torch.stack([r, c]), v, (3 * N, 3 * N)).coalesce()
+    return A.to_sparse_csr()
+
+
+def gain_samples(count=16, n=64, seed=777, iterates=(1, 2, 4, 8), log=None):
+    """Residual samples for train_gain: per random polycrystal problem (as in
+    training_samples) the residuals r_k of the k-th FP64 F-cycle iterate
+    from x = 0, the image w = A M r_k of the multigrid direction on that
+    residual (M one F-cycle), the operator A as a sparse matrix and the GCR
+    weights 1/diag^2.  Each problem: {A, At, W, h2, items: [(feat, r, rms,
+    w)]}."""
+    import torch
+    from . import microstructure as M
+    from .elastic import TensionTest
+    rng = np.random.default_rng(seed)
+    N = (n + 1) ** 3
+    out = []
+    for q in range(count):
+        ng = int(rng.integers(8, 65))
+        ddw, _, _ = M.voronoi_cubic_device(n, ngrains=ng, seed=int(rng.integers(1, 2 ** 31)))
+        op = Elastic([n] * 3, None, "majorminor")
+        op.SetBC(TensionTest("uniaxial_stress", disp=0.01))
+        op.SetModel(ddw)
+        del ddw
+        zero = torch.zeros(3 * N, dtype=torch.float64, device="cuda")
+        b = op.BCInit(torch.zeros(3 * N, dtype=torch.float64, device="cuda"))
+        rhs = torch.empty(3 * N, dtype=torch.float64, device="cuda")
+        op.NewtonRHS(zero, b, out=rhs)
+        A = operator_matrix(op)
+        D = op.Diagonal(0, out=torch.empty(3 * N, dtype=torch.float64, device="cuda"))
+        items = []
+        for k in iterates:
+            s = Linear(op, fixed_iter=k, max_iter=k)
+            xk = torch.zeros(3 * N, dtype=torch.float64, device="cuda")
+            s.solve(xk, rhs, 1e-30, 0.0, raise_on_fail=False)
+            s.Clear()
+            rk = torch.empty(3 * N, dtype=torch.float64, device="cuda")
+            op.solutionResidual(0, xk, rhs, out=rk)
+            feat, rms = features(op, rk)
+            one = Linear(op, fixed_iter=1, max_iter=1)
+            zm = torch.zeros(3 * N, dtype=torch.float64, device="cuda")
+            one.solve(zm, rk, 1e-30, 0.0, raise_on_fail=False)
+            one.Clear()
+            items.append((feat, rk, rms, A @ zm))
+        out.append({"A": A, "At": A.t().to_sparse_csr(), "W": 1.0 / D ** 2, "h2": (1.0 / n) ** 2, "items": items})
+        op.close()
+        if log and (q + 1) % max(1, count // 4) == 0:
+            log("gain samples: %d of %d problems" % (q + 1, count))
+    return out
+
+
+def _wproj_out(v, w, W):
+    """v minus its weighted projection on w."""
+    ww = (w * w * W).sum()
+    return v - ((v * w * W).sum() / ww) * w if float(ww) > 0 else v
+
+
+def gcr_gain(A, W, z, r, w=None):
+    """The fraction of ||r||_W^2 one GCR step along z removes,
+    <A z, r>_W^2 / (<A z, A z>_W <r, r>_W); with w (the image of the
+    multigrid direction on the same residual), the fraction of what the
+    multigrid direction leaves that z removes on top of it: r and A z are
+    first made W-orthogonal to w, as the solve's GCR makes them."""
+    az = A @ z
+    if w is not None:
+        r = _wproj_out(r, w, W)
+        az = _wproj_out(az, w, W)
+    return float((az * r * W).sum() ** 2 / ((az * az * W).sum() * (r * r * W).sum()))
+
+
+def train_gain(net, problems, n, steps=600, lr=1e-3, warmup=50, log=None):
+    """Adam on 1 - gain with gain the fraction of the residual the
+    multigrid direction leaves that the network's direction removes on top
+    of it (gcr_gain with w): z the network's correction of a residual r
+    (out[:, 0:3] times rms h^2 in the reference layout), A z and r made
+    W-orthogonal to w = A M r; the gradient with respect to z is A^T of the
+    gradient with respect to A z (torch autograd through the projection).
+    One residual per step, cycling over problems and iterates.  Returns the
+    history of the gain."""
+    import torch
+    g0 = (n + 1,) * 3
+    V = (n + 1) ** 3
+    items = [(p, it) for p in problems for it in p["items"]]
+    hist = []
+    for step in range(steps):
+        p, (feat, r, rms, w) = items[step % len(items)]
+        W = p["W"]
+        out = net.forward(g0, feat)
+        scale = rms * p["h2"]
+        z = out[:, :3].double().t().reshape(-1) * scale   # reference layout
+        az = (p["A"] @ z).detach().requires_grad_(True)
+        rp = _wproj_out(r, w, W)
+        y = _wproj_out(az, w, W)
+        a = (y * rp * W).sum()
+        gain = a * a / ((y * y * W).sum() * (rp * rp * W).sum())
+        (1.0 - gain).backward()
+        hist.append(float(gain.detach()))
+        gaz = az.grad if az.grad is not None else torch.zeros_like(az)
+        gz = p["At"] @ torch.nan_to_num(gaz)
+        dout = torch.zeros(V, FEAT, dtype=torch.float32, device="cuda")
+        dout[:, :3] = (gz.reshape(3, V).t() * scale).float()
+        gw, gb = net.backward(g0, dout)
+        net.adam(gw, gb, lr=lr * min(1.0, (step + 1) / float(warmup)))
+        if log and (step + 1) % max(1, steps // 10) == 0:
+            log("step %d: mean gain over the last 50 steps %.4f" % (step + 1, float(np.mean(hist[-50:]))))
     return hist

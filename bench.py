@@ -53,14 +53,15 @@ def parse():
     ap.add_argument("--cycle", default="F", choices=["F", "V"])
     ap.add_argument("--krylov", type=int, default=8,
                     help="c2, rve: stored directions of the flexible GCR over the FP32 cycle (0: the FP32 cycles alone)")
-    ap.add_argument("--workload", default="c2", choices=["c2", "rve", "learned", "sweep"],
+    ap.add_argument("--workload", default="c2", choices=["c2", "rve", "learned", "sweep", "conv"],
                     help="c2: the 257^3 polycrystal (default); rve: batched periodic RVEs; learned: the learned "
                          "correction trained on 64^3 polycrystals and evaluated on the c2 system at 129^3 and 257^3; sweep: the finest-level "
-                         "operator kernels of the c2 system alone (Fapply, residual, Jacobi; FP32 and FP64)")
+                         "operator kernels of the c2 system alone (Fapply, residual, Jacobi; FP32 and FP64); conv: the "
+                         "learned network's tensor-core convolutions and its forward pass on an (n+1)^3 grid")
     ap.add_argument("--rves", type=int, default=512, help="rve workload: number of RVEs")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "f64"], help="rve workload")
-    ap.add_argument("--train-problems", type=int, default=48, help="learned workload: 64^3 training problems")
-    ap.add_argument("--train-steps", type=int, default=600, help="learned workload: Adam steps")
+    ap.add_argument("--train-problems", type=int, default=16, help="learned workload: 64^3 training problems")
+    ap.add_argument("--train-steps", type=int, default=2000, help="learned workload: Adam steps")
     return ap.parse_args()
 
 
@@ -374,6 +375,68 @@ def run_sweep(args, dist):
     dist.close()
 
 
+def run_conv(args, dist):
+    """The learned network's 3x3x3 tensor-core convolutions (tcgen05) timed
+    alone, one shape per layer of the U-Net on its grid of an (n+1)^3-node
+    box, and the whole forward pass: `--steps` back-to-back launches after
+    one warm-up, CUDA events.  FLOP/s = 2 x 27 cin cout per voxel against the
+    measured BF16 peak; GB/s from the activations read and written once."""
+    import ctypes
+    import torch
+    from alamo_gb300._lib import check, lib
+    from alamo_gb300.learned import UNet, _i3, _vp, grids
+    torch.cuda.set_device(dist.local)
+    L = lib()
+    g0 = (args.n + 1,) * 3
+    G = grids(g0)
+    peak = None
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peak = float(json.load(f)["bf16_tflops"])
+    except Exception:
+        peak = 1900.0
+    reps = max(1, args.steps)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    out = {}
+    net = UNet(seed=0)
+    for l, (ci, co, lev) in enumerate(zip(net.cin, net.cout, net.lev)):
+        g = G[lev]
+        V = int(np.prod(g))
+        x = torch.randn(V * ci, device="cuda").to(torch.bfloat16)
+        y = torch.empty(V * co, dtype=torch.bfloat16, device="cuda")
+        wp = torch.empty(27 * co * ci, dtype=torch.bfloat16, device="cuda")
+        check(L.agb_conv3_tc_pack(ci, co, _vp(net.wb[l]), co, 0, _vp(wp), None))
+
+        def run():
+            check(L.agb_conv3_tc(_i3(g), ci, co, _vp(x), ci, 0, _vp(wp), _vp(net.b[l]), _vp(y), co, 0, 0, 1, None))
+        run()
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            run()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        tf = 2.0 * 27 * ci * co * V / ms / 1e9
+        out["layer%d_%dx%d_%d^3" % (l, ci, co, g[0])] = {"ms": round(ms, 4), "tflops": round(tf, 1),
+                                                          "frac_bf16": round(tf / peak, 4),
+                                                          "gbs": round(V * (ci + co) * 2 / ms / 1e6, 1)}
+    feat = torch.randn(int(np.prod(G[0])), 16, device="cuda").to(torch.bfloat16)
+    net.forward(g0, feat)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(reps):
+        net.forward(g0, feat)
+    e1.record()
+    torch.cuda.synchronize()
+    line = {"metric": "learned network: tcgen05 convolutions and forward pass", "workload": "conv", "n": args.n,
+            "bf16_peak_tflops": peak, "forward_ms": round(e0.elapsed_time(e1) / reps, 3), "layers": out}
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    net.close()
+    dist.close()
+
+
 def run_rve(args, dist):
     """Batched RVE homogenization: `--rves` periodic RVEs (edges 32-96 cells,
     diffuse ellipsoidal inclusions, contrast up to 100, uniform eigenstrain),
@@ -436,29 +499,29 @@ def run_rve(args, dist):
 
 
 def run_learned(args, dist):
-    """Learned correction: the U-Net trained (untimed) on multigrid samples of
-    random 64^3 cubic polycrystals, then the c2 system at 129^3 and 257^3
+    """Learned correction: the U-Net trained (untimed) on the GCR gain of
+    multigrid residuals of random 64^3 cubic polycrystals, then the c2 system at 129^3 and 257^3
     nodes solved by the benchmark's method (FP32 F-cycles under GCR(8) in
     FP64 refinement) with and without the network's directions (the
     ablation), and by plain FP64 multigrid; solve times are device times of
     the best of two solves."""
     import torch
     from alamo_gb300 import Elastic, Linear
-    from alamo_gb300.learned import UNet, learned_stats, train, training_samples
+    from alamo_gb300.learned import UNet, gain_samples, learned_stats, train_gain
     torch.cuda.set_device(dist.local)
     log = lambda m: print(m, file=sys.stderr, flush=True)
     t0 = time.perf_counter()
-    samples = training_samples(count=args.train_problems, n=64, seed=777, log=log)
+    problems = gain_samples(count=args.train_problems, n=64, seed=777, log=log)
     t1 = time.perf_counter()
     net = UNet(seed=1)
-    hist = train(net, samples, 64, steps=args.train_steps, lr=1e-3, warmup=50, log=log)
+    hist = train_gain(net, problems, 64, steps=args.train_steps, lr=1e-3, warmup=50, log=log)
     torch.cuda.synchronize()
     t2 = time.perf_counter()
-    del samples
-    out = {"train": {"problems": args.train_problems, "samples": 3 * args.train_problems, "n": 64,
-                     "steps": args.train_steps, "params": net.nparams(), "data_s": round(t1 - t0, 1),
-                     "train_s": round(t2 - t1, 1), "loss_first50": float(np.mean(hist[:50])),
-                     "loss_last50": float(np.mean(hist[-50:]))}}
+    nsamples = sum(len(p["items"]) for p in problems)
+    del problems
+    out = {"train": {"problems": args.train_problems, "samples": nsamples, "n": 64, "steps": args.train_steps,
+                     "params": net.nparams(), "data_s": round(t1 - t0, 1), "train_s": round(t2 - t1, 1),
+                     "gain_first50": float(np.mean(hist[:50])), "gain_last50": float(np.mean(hist[-50:]))}}
     for n in (128, 256):
         ddw_h, bc = workload(n, args.grains)
         op = Elastic([n] * 3, None, "majorminor")
@@ -496,8 +559,8 @@ def run_learned(args, dist):
             "value": out["257^3"]["mixed_gcr8_learned"]["ms"] / 1000.0, "unit": "s", "n_gpus": 1, "steps": 2,
             "warmup": 0, "higher_is_better": False, "dtype": "bf16 net + f32/f64 solve",
             "data": "synthetic (seeded Voronoi polycrystals)",
-            "config": {"workload": "U-Net trained on %d multigrid samples of 64^3 cubic polycrystals, "
-                                   "evaluated on the 129^3 and 257^3 c2 systems" % (3 * args.train_problems)},
+            "config": {"workload": "U-Net trained on the GCR gain of %d multigrid residuals of 64^3 cubic "
+                                   "polycrystals, evaluated on the 129^3 and 257^3 c2 systems" % nsamples},
             "learned": out}
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
@@ -515,6 +578,8 @@ def main():
         return run_learned(args, dist)
     if args.workload == "sweep":
         return run_sweep(args, dist)
+    if args.workload == "conv":
+        return run_conv(args, dist)
     res, ddw_h, bc = run_ours(args, dist)
     peak, peak_kind = measured_peak_hbm()
     nodes = res["nodes"]
