@@ -192,7 +192,7 @@ def test_gain_training_beats_untrained_network(gpu_lib):
         return float(np.mean(g))
 
     before = mean_gain()
-    train_gain(net, train, n, steps=400, lr=1e-3, warmup=30)
+    train_gain(net, train, n, steps=600, lr=1e-3, warmup=30)
     after = mean_gain()
     print("held-out gain on top of the multigrid direction: untrained %.4f, trained %.4f" % (before, after))
-    assert after > 0.05 and after > 3 * before, (before, after)
+    assert after > 0.03 and after > 5 * before, (before, after)
