@@ -120,6 +120,7 @@ def lib():
                               ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp]),
         "agb_conv3_tc_error": (st, [ctypes.POINTER(ctypes.c_int)]),
         "agb_op_time_sweep": (st, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]),
+        "agb_fp64_fma_peak": (st, [ctypes.c_int, dp, ctypes.POINTER(ctypes.c_float)]),
         "agb_host_alloc": (st, [ctypes.c_size_t, ctypes.POINTER(vp)]),
         "agb_host_free": (st, [vp]),
         "agb_conv3_flip": (st, [ctypes.c_int, ctypes.c_int, vp, vp, vp]),

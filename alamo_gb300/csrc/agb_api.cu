@@ -79,6 +79,14 @@ long long& launch_counter()
     return n;
 }
 void set_error(const char* msg) { g_err = msg ? msg : ""; }
+bool pdl_enabled()
+{
+    static bool v = [] {
+        const char* s = getenv("AGB_PDL");
+        return !(s && s[0] == '0');
+    }();
+    return v;
+}
 int sm_count()
 {
     static int cache[64] = {0};
@@ -113,6 +121,8 @@ struct agb_op_s {
     double* h_slots = nullptr;   // pinned mirror
     double* bottom_work = nullptr;
     double* bottom_A = nullptr;   // dense coarsest-level operator (small bottom levels)
+    float* bottom_inv32 = nullptr;   // its inverse for the FP32 cycles (exact coarsest solve)
+    int* bottom_inv_ok = nullptr;    // device flag: the inverse exists
     int* d_ret = nullptr;
     char* stage = nullptr;       // bounded staging buffer for pageable host copies
     size_t stage_bytes = 0;
@@ -339,6 +349,9 @@ agb_status ensure_f32(agb_op op)
         launch_convert<float, double>(op->st, lv.L, op->nc, lv.ddw64, lv.ddw32, 1.0);
         launch_recip<float>(op->st, lv.L, 3, lv.diag64, lv.dinv32);
     }
+    // prepare() assembled the dense coarsest operator; the FP32 cycles take its inverse
+    if (op->bottom_inv32)
+        launch_bottom_invert(op->st, op->lev.back().L, op->bottom_A, op->bottom_inv32, op->bottom_inv_ok);
     CK(cudaGetLastError());
     op->f32_ready = true;
     return AGB_OK;
@@ -386,6 +399,7 @@ agb_status prepare_mixed(agb_op op)
     launch_recip<double>(op->st, bl.L, 3, bl.diag64, bl.dinv64);
     if (op->bottom_A)
         launch_bottom_assemble(op->st, op->sym, bl.L, op->bc, op->uniform, bl.ddw64, op->bottom_A);
+    if (op->bottom_inv32) launch_bottom_invert(op->st, bl.L, op->bottom_A, op->bottom_inv32, op->bottom_inv_ok);
     CK(cudaGetLastError());
     op->prepared = false;
     op->f32_ready = true;
@@ -467,6 +481,20 @@ template <typename T> struct Engine {
     {
         for (int s = 0; s < nsmooth; s++) sweep2(l, x, b);
     }
+    // x = 0, then Fsmooth: the first sweep of a zero guess is elementwise
+    // (launch_jacobi_zero), the rest are stencil sweeps
+    void smooth_from_zero(int l, T* x, const T* b, int nsmooth)
+    {
+        Level& v = lv(l);
+        if (nsmooth <= 0) {
+            launch_zero<T>(op->st, v.L, 3, x);
+            return;
+        }
+        launch_jacobi_zero<T>(op->st, v.L, 3, A::tmp(v), b, A::dinv(v), (T)op->omega);
+        launch_stencil<T>(op->st, op->sym, MODE_JACOBI, v.L, op->bc, op->uniform, A::ddw(v), A::tmp(v), b,
+                          A::dinv(v), x, (T)op->omega, nullptr);
+        for (int s = 1; s < nsmooth; s++) sweep2(l, x, b);
+    }
     void residual(int l, const T* x, const T* b, T* r, void* slot)
     {
         Level& v = lv(l);
@@ -491,9 +519,13 @@ template <typename T> struct Engine {
     {
         Level& v = lv(bot());
         if (op->bottom_A) {
+            // the FP32 cycles of the mixed solve take the exact coarsest solve
+            // when prepare_mixed made the inverse; the FP64 cycles keep MLMG's
+            // BiCGStab bottom
+            const bool exact = sizeof(T) == 4 && op->bottom_inv32 && op->f32_ready;
             launch_bottom_dense<T>(op->st, v.L, op->bottom_A, v.diag64, A::cor(v), A::res(v), p.bottom_max_iter,
                                    p.bottom_tol_rel, p.bottom_tol_abs, op->d_ret, p.bottom_smooth, p.final_smooth,
-                                   op->omega);
+                                   op->omega, exact ? op->bottom_inv32 : nullptr, exact ? op->bottom_inv_ok : nullptr);
             return;
         }
         launch_bottom<T>(op->st, op->sym, v.L, op->bc, op->uniform, v.ddw64, v.diag64, A::cor(v), A::res(v),
@@ -506,8 +538,7 @@ template <typename T> struct Engine {
         const int b = bot();
         for (int l = top; l < b; l++) {
             Level& v = lv(l);
-            launch_zero<T>(op->st, v.L, 3, A::cor(v));
-            smooth(l, A::cor(v), A::res(v), p.pre_smooth);
+            smooth_from_zero(l, A::cor(v), A::res(v), p.pre_smooth);
             residual(l, A::cor(v), A::res(v), A::rescor(v), nullptr);
             launch_restriction<T>(op->st, v.L, lv(l + 1).L, A::rescor(v), A::res(lv(l + 1)), 3);
         }
@@ -1015,6 +1046,7 @@ agb_status agb_op_create(const int n_cells[3], const double dx[3], const int per
     };
     if (cudaStreamCreateWithFlags(&op->st, cudaStreamNonBlocking) != cudaSuccess)
         return bail(fail(AGB_CUDA, "cudaStreamCreate failed"));
+    register_side_stream(op->st);
     cudaEventCreate(&op->e0);
     cudaEventCreate(&op->e1);
     if (!g_attr_done) {
@@ -1057,6 +1089,11 @@ agb_status agb_op_create(const int n_cells[3], const double dx[3], const int per
     if (bottom_dense_fits(op->lev.back().L) && use_dense_bottom()) {
         if ((s = op->alloc(&op->bottom_A, bottom_dense_bytes(op->lev.back().L) / sizeof(double))) != AGB_OK)
             return bail(s);
+        if (use_exact_bottom()) {
+            if ((s = op->alloc(&op->bottom_inv32, bottom_dense_bytes(op->lev.back().L) / sizeof(double))) != AGB_OK)
+                return bail(s);
+            if ((s = op->alloc(&op->bottom_inv_ok, 1)) != AGB_OK) return bail(s);
+        }
     }
     op->stage_bytes = 64u << 20;
     if ((s = op->alloc(&op->stage, op->stage_bytes)) != AGB_OK) return bail(s);
@@ -1076,7 +1113,10 @@ agb_status agb_op_destroy(agb_op op)
     if (op->h_slots) cudaFreeHost(op->h_slots);
     if (op->e0) cudaEventDestroy(op->e0);
     if (op->e1) cudaEventDestroy(op->e1);
-    if (op->st) cudaStreamDestroy(op->st);
+    if (op->st) {
+        unregister_side_stream(op->st);
+        cudaStreamDestroy(op->st);
+    }
     delete op;
     return AGB_OK;
 }

@@ -195,6 +195,23 @@ template <typename T> struct BEngine {
                                     (T)b->omega, nullptr);
         }
     }
+    // x = 0, then the smoothing: the first sweep of a zero guess is
+    // elementwise (BV_JACOBI0), the rest are stencil sweeps
+    void smooth_from_zero(int l, T* x, const T* rhs, int ns)
+    {
+        BLevel& v = b->lev[l];
+        if (ns <= 0 || v.tS_smooth.empty()) {
+            launch_batch_vec(b->st, BV_ZERO, b->grid, v.d_probs, v.c_t32_smooth, (int)v.t32_smooth.size(), act, x,
+                             nullptr, 0.0, nullptr, fp32);
+            return;
+        }
+        launch_batch_vec(b->st, BV_JACOBI0, b->grid, v.d_probs, v.c_t32_smooth, (int)v.t32_smooth.size(), act,
+                         A::tmp(v), rhs, b->omega, nullptr, fp32, A::dinv(v));
+        launch_batch_stencil<T>(b->st, b->sym, MODE_JACOBI, v.shape, b->grid, v.d_probs, v.c_tS_smooth,
+                                (int)v.tS_smooth.size(), act, b->bc, false, A::ddw(v), A::tmp(v), rhs, A::dinv(v), x,
+                                (T)b->omega, nullptr);
+        smooth(l, x, rhs, ns - 1);
+    }
     // MLMG::mgVcycle(0, 0) for every problem, each with its own bottom level
     void vcycle() { vcycle_from(0, false); }
     // MLMG::mgVcycle(0, top) for the problems that have level top; with
@@ -206,9 +223,7 @@ template <typename T> struct BEngine {
         for (int l = top; l < L; l++) {
             BLevel& v = b->lev[l];
             if (!v.t32_smooth.empty()) {
-                launch_batch_vec(b->st, BV_ZERO, b->grid, v.d_probs, v.c_t32_smooth, (int)v.t32_smooth.size(), act,
-                                 A::cor(v), nullptr, 0.0, nullptr, fp32);
-                smooth(l, A::cor(v), A::res(v), b->p.pre_smooth);
+                smooth_from_zero(l, A::cor(v), A::res(v), b->p.pre_smooth);
                 launch_batch_stencil<T>(b->st, b->sym, MODE_RESID, v.shape, b->grid, v.d_probs, v.c_tS_smooth,
                                         (int)v.tS_smooth.size(), act, b->bc, false, A::ddw(v), A::cor(v), A::res(v),
                                         nullptr, A::rescor(v), (T)0, nullptr);

@@ -84,6 +84,45 @@ void set_error(const char* msg);
 
 enum StencilMode { MODE_APPLY = 0, MODE_RESID = 1, MODE_JACOBI = 2 };
 
+// Programmatic dependent launch.  The multigrid cycle is a chain of short
+// kernels on one stream; launched by pdl_launch, a kernel may be scheduled
+// while the kernel before it drains, so its launch and prologue overlap that
+// kernel's tail.  Every kernel launched so starts with pdl_entry():
+// griddepcontrol.wait returns once the preceding grid has completed and its
+// writes are visible (so nothing the kernel reads or writes is touched
+// before), then launch_dependents lets the next kernel of the chain be
+// scheduled.  Launched without the attribute both are no-ops.  AGB_PDL=0
+// launches without it.
+__device__ __forceinline__ void pdl_entry()
+{
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+bool pdl_enabled();
+
+// A side stream bound to an operator's stream: the boundary shell of a big
+// level's stencil sweep runs on it, forked from and joined back into the main
+// stream, so it overlaps the interior kernel (they write disjoint nodes).
+// Registered when the operator is created (outside any graph capture);
+// launches on an unregistered stream run the two kernels in order.
+void register_side_stream(cudaStream_t main);
+void unregister_side_stream(cudaStream_t main);
+template <typename... KArgs, typename... Args>
+inline void pdl_launch(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, Args... args)
+{
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = pdl_enabled() ? 1 : 0;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 // ---------------------------------------------------------------------------
 // Batched solves: many independent boxes of different sizes per level.
 // Each problem's fields of one level live back to back in a level arena;
@@ -106,7 +145,7 @@ struct BTile {
     short pad;
 };
 
-enum BatchVecOp { BV_ZERO = 0, BV_COPY = 1, BV_AXPY = 2, BV_SCALE_TO32 = 3, BV_ACC_FROM32 = 4 };
+enum BatchVecOp { BV_ZERO = 0, BV_COPY = 1, BV_AXPY = 2, BV_SCALE_TO32 = 3, BV_ACC_FROM32 = 4, BV_JACOBI0 = 5 };
 
 template <typename T>
 void launch_batch_stencil(cudaStream_t st, int sym, int mode, int shape, int grid, const BProb* probs,
@@ -120,7 +159,8 @@ void launch_batch_avg_ddw(cudaStream_t st, int grid, const BProb* pf, const BPro
 void launch_batch_diag(cudaStream_t st, int sym, int grid, const BProb* probs, const BTile* tiles, int ntiles,
                        const BCTable& bc, const double* ddw, double* diag, double* dinv64, float* dinv32);
 void launch_batch_vec(cudaStream_t st, int op, int grid, const BProb* probs, const BTile* tiles, int ntiles,
-                      const int* active, void* y, const void* x, double a, const double* scale, int fp32);
+                      const int* active, void* y, const void* x, double a, const double* scale, int fp32,
+                      const void* x2 = nullptr);
 void launch_batch_bottom(cudaStream_t st, int sym, int fp32, const BProb* probs, const int* plist, int np,
                          const int* active, const BCTable& bc, bool uniform, const void* ddw, const double* diag,
                          void* cor, const void* res, double* work, int maxiter, double tol_rel, double tol_abs, int nub,
@@ -173,6 +213,9 @@ template <typename T>
 void launch_axpy(cudaStream_t st, const LevelDesc& L, int ncomp, T* y, const T* x, T a);
 template <typename T>
 void launch_zero(cudaStream_t st, const LevelDesc& L, int ncomp, T* y);
+// out = omega (b / D): the first damped-Jacobi sweep from a zero guess
+template <typename T>
+void launch_jacobi_zero(cudaStream_t st, const LevelDesc& L, int ncomp, T* out, const T* b, const T* dinv, T omega);
 template <typename T>
 void launch_norm_inf(cudaStream_t st, const LevelDesc& L, int ncomp, const T* x, void* norm_slot);
 
@@ -237,16 +280,19 @@ int tma_error_take();   // 1 if a TMA kernel's bounded wait ran out since the la
 void init_tma_attributes();
 
 // Dense coarsest level (at most 128 unknowns): A assembled once per solve,
-// BiCGStab + smoothing of launch_bottom on it in one warp.
+// BiCGStab + smoothing of launch_bottom on it in one CTA; or, with inv and
+// *inv_ok set (launch_bottom_invert), the exact product cor = A^-1 res.
 bool bottom_dense_fits(const LevelDesc& L);
 bool use_dense_bottom();
+bool use_exact_bottom();
 size_t bottom_dense_bytes(const LevelDesc& L);
 void launch_bottom_assemble(cudaStream_t st, int sym, const LevelDesc& L, const BCTable& bc, bool uniform,
                             const double* ddw64, double* A);
+void launch_bottom_invert(cudaStream_t st, const LevelDesc& L, const double* A, float* inv, int* ok);
 template <typename T>
 void launch_bottom_dense(cudaStream_t st, const LevelDesc& L, const double* A, const double* diag64, T* cor,
                          const T* res, int maxiter, double tol_rel, double tol_abs, int* ret_slot, int nub, int nuf,
-                         double omega);
+                         double omega, const float* inv = nullptr, const int* inv_ok = nullptr);
 void init_bottom_attributes();
 template <typename T>
 void launch_bottom(cudaStream_t st, int sym, const LevelDesc& L, const BCTable& bc, bool uniform,

@@ -625,8 +625,9 @@ __global__ void __launch_bounds__(256) k_batch_diag(const BProb* __restrict__ pr
         const long long p = L.idx(i, j, k);
         double c[NCoef<SYM>::value];
         for (int m = 0; m < NCoef<SYM>::value; m++) c[m] = ddw[P.co + m * L.S + p];
+        const DiagGeo<double> dg = make_diag_geo<double>(L);
         for (int q = 0; q < 3; q++) {
-            const double d = diag_entry<double, SYM>(c, L, bc, mn, mx, q);
+            const double d = diag_entry<double, SYM>(c, L, dg, bc, mn, mx, q);
             const long long o = P.vo + q * L.S + p;
             diag[o] = d;
             dinv64[o] = d != 0.0 ? 1.0 / d : 0.0;
@@ -641,10 +642,13 @@ __global__ void __launch_bounds__(256) k_batch_diag(const BProb* __restrict__ pr
 //   BV_AXPY        y += a x
 //   BV_SCALE_TO32  y(float) = x(double) / scale[prob]
 //   BV_ACC_FROM32  y(double) += x(float) * scale[prob]
+//   BV_JACOBI0     y = a (x * x2): the first damped-Jacobi sweep from a zero
+//                  guess (x the right-hand side, x2 = 1/D, a = omega), the
+//                  sweep kernels' expression with A 0 = 0
 __global__ void __launch_bounds__(256) k_batch_vec(int op, const BProb* __restrict__ probs,
                                                    const BTile* __restrict__ tiles, int ntiles,
                                                    const int* __restrict__ active, void* y, const void* x, double a,
-                                                   const double* __restrict__ scale, int fp32)
+                                                   const double* __restrict__ scale, int fp32, const void* x2)
 {
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const BTile tl = tiles[t];
@@ -665,12 +669,14 @@ __global__ void __launch_bounds__(256) k_batch_vec(int op, const BProb* __restri
                 const float* xx = (const float*)x;
                 if (op == BV_ZERO) yy[q] = 0.f;
                 else if (op == BV_COPY) yy[q] = xx[q];
+                else if (op == BV_JACOBI0) yy[q] = (float)a * (xx[q] * ((const float*)x2)[q]);
                 else yy[q] += (float)a * xx[q];
             } else {
                 double* yy = (double*)y;
                 const double* xx = (const double*)x;
                 if (op == BV_ZERO) yy[q] = 0.0;
                 else if (op == BV_COPY) yy[q] = xx[q];
+                else if (op == BV_JACOBI0) yy[q] = a * (xx[q] * ((const double*)x2)[q]);
                 else yy[q] += a * xx[q];
             }
         }
@@ -1160,10 +1166,11 @@ void launch_batch_diag(cudaStream_t st, int sym, int grid, const BProb* probs, c
 }
 
 void launch_batch_vec(cudaStream_t st, int op, int grid, const BProb* probs, const BTile* tiles, int ntiles,
-                      const int* active, void* y, const void* x, double a, const double* scale, int fp32)
+                      const int* active, void* y, const void* x, double a, const double* scale, int fp32,
+                      const void* x2)
 {
     grid = fit_grid((const void*)k_batch_vec, grid, st);
-    k_batch_vec<<<grid, 256, 0, st>>>(op, probs, tiles, ntiles, active, y, x, a, scale, fp32);
+    k_batch_vec<<<grid, 256, 0, st>>>(op, probs, tiles, ntiles, active, y, x, a, scale, fp32, x2);
     count_launch();
 }
 

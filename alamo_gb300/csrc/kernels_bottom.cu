@@ -537,16 +537,39 @@ template <typename R> __device__ __forceinline__ void dense_load(R* A, const dou
     for (int q = threadIdx.x; q < nu * nu; q += blockDim.x) A[q] = (R)Ag[q];
 }
 
+// With `inv` set and *inv_ok (an exact inverse exists, k_bottom_invert), the
+// bottom is the product cor = A^-1 res instead of the BiCGStab solve.
 template <typename T, typename R>
 __global__ void __launch_bounds__(DENSE_MAX) k_bottom_dense(LevelDesc L, const double* __restrict__ Ag,
                                                             const double* __restrict__ diag, T* __restrict__ cor,
                                                             const T* __restrict__ res, int maxiter, double eps_rel_d,
                                                             double eps_abs_d, int nub, int nuf, double omega_d,
-                                                            int* ret_slot)
+                                                            int* ret_slot, const float* __restrict__ inv,
+                                                            const int* __restrict__ inv_ok)
 {
+    pdl_entry();
     extern __shared__ __align__(16) unsigned char dsm_raw[];
     __shared__ R red[2 * 3 * 32];
-    const int nu = 3 * (int)L.count();
+    const int cnt = (int)L.count(), nu = 3 * cnt;
+    if (inv && *inv_ok) {
+        float* xs = reinterpret_cast<float*>(dsm_raw);
+        const int q = threadIdx.x;
+        const long long pq = q < nu ? dense_to_padded(L, q, cnt) : 0;
+        if (q < nu) xs[q] = (float)__ldcg(res + pq);
+        __syncthreads();
+        if (q < nu) {
+            float y0 = 0.0f, y1 = 0.0f;
+            int j = 0;
+            for (; j + 1 < nu; j += 2) {
+                y0 = fmaf(inv[(long long)j * nu + q], xs[j], y0);
+                y1 = fmaf(inv[(long long)(j + 1) * nu + q], xs[j + 1], y1);
+            }
+            if (j < nu) y0 = fmaf(inv[(long long)j * nu + q], xs[j], y0);
+            cor[pq] = (T)(y0 + y1);
+        }
+        if (threadIdx.x == 0 && ret_slot) *ret_slot = 0;
+        return;
+    }
     R* A = reinterpret_cast<R*>(dsm_raw);
     dense_load<R>(A, Ag, nu);
     __syncthreads();
@@ -555,6 +578,130 @@ __global__ void __launch_bounds__(DENSE_MAX) k_bottom_dense(LevelDesc L, const d
 }
 
 bool bottom_dense_fits(const LevelDesc& L) { return 3 * L.count() <= DENSE_MAX; }
+
+// ---------------------------------------------------------------------------
+// Exact coarsest solve for the FP32 cycles of the mixed solve.  Once per solve
+// the dense operator (FP64, column-major) is inverted by Gauss-Jordan
+// elimination with partial pivoting in one CTA, the matrix in shared memory
+// (row-major), and stored in FP32 column-major (inv[j * nu + r] = A^-1(r, j))
+// so that thread r of the product reads a coalesced column per j.  A fully
+// periodic level (singular), or a pivot at or below 1e-13 of the largest
+// |entry|, clears *ok and the cycles keep the BiCGStab bottom.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(1024) k_bottom_invert(LevelDesc L, const double* __restrict__ Ag,
+                                                       float* __restrict__ inv, int* __restrict__ ok)
+{
+    extern __shared__ __align__(16) unsigned char inv_raw[];
+    double* M = reinterpret_cast<double*>(inv_raw);   // nu x nu, row-major
+    __shared__ double fcol[DENSE_MAX];
+    __shared__ int piv[DENSE_MAX];
+    __shared__ double amax_s, pinv_s;
+    __shared__ int bad_s;
+    const int nu = 3 * (int)L.count();
+    const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31;
+    if (L.singular() || nu > DENSE_MAX) {
+        if (tid == 0) *ok = 0;
+        return;
+    }
+    double a = 0.0;
+    for (int t = tid; t < nu * nu; t += nt) {
+        const double v = Ag[t];
+        M[(t % nu) * nu + t / nu] = v;
+        a = fmax(a, fabs(v));
+    }
+    // block max of |A| (every warp's lane 0 folds into amax_s)
+    for (int o = 16; o > 0; o >>= 1) a = fmax(a, __shfl_xor_sync(0xffffffffu, a, o));
+    if (tid == 0) {
+        amax_s = 0.0;
+        bad_s = 0;
+    }
+    __syncthreads();
+    if (lane == 0) atomicMax(reinterpret_cast<unsigned long long*>(&amax_s), (unsigned long long)__double_as_longlong(a));
+    __syncthreads();
+    const double tol = 1e-13 * amax_s;
+    for (int k = 0; k < nu; k++) {
+        if (tid < 32) {
+            // pivot: the largest |M(r, k)| for r >= k (ties to the lower row)
+            double best = -1.0;
+            int br = k;
+            for (int r = k + lane; r < nu; r += 32) {
+                const double v = fabs(M[r * nu + k]);
+                if (v > best) {
+                    best = v;
+                    br = r;
+                }
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+                const int orow = __shfl_xor_sync(0xffffffffu, br, o);
+                if (ob > best || (ob == best && orow < br)) {
+                    best = ob;
+                    br = orow;
+                }
+            }
+            if (lane == 0) {
+                piv[k] = br;
+                if (!(best > tol)) bad_s = 1;
+            }
+        }
+        __syncthreads();
+        if (bad_s) break;   // uniform: every thread reads it after the barrier
+        const int pr = piv[k];
+        if (pr != k)
+            for (int c = tid; c < nu; c += nt) {
+                const double t = M[k * nu + c];
+                M[k * nu + c] = M[pr * nu + c];
+                M[pr * nu + c] = t;
+            }
+        __syncthreads();
+        if (tid == 0) pinv_s = 1.0 / M[k * nu + k];
+        __syncthreads();
+        const double pinv = pinv_s;
+        for (int c = tid; c < nu; c += nt) M[k * nu + c] = (c == k ? 1.0 : M[k * nu + c]) * pinv;
+        for (int r = tid; r < nu; r += nt) fcol[r] = r == k ? 0.0 : M[r * nu + k];
+        __syncthreads();
+        for (int t = tid; t < nu * nu; t += nt) {
+            const int r = t / nu, c = t - r * nu;
+            if (r == k) continue;
+            M[t] = (c == k ? 0.0 : M[t]) - fcol[r] * M[k * nu + c];
+        }
+        __syncthreads();
+    }
+    if (bad_s) {
+        if (tid == 0) *ok = 0;
+        return;
+    }
+    // undo the row interchanges: swap columns k <-> piv[k], last interchange first
+    for (int k = nu - 1; k >= 0; k--) {
+        const int pc = piv[k];
+        if (pc != k)
+            for (int r = tid; r < nu; r += nt) {
+                const double t = M[r * nu + k];
+                M[r * nu + k] = M[r * nu + pc];
+                M[r * nu + pc] = t;
+            }
+        __syncthreads();
+    }
+    for (int t = tid; t < nu * nu; t += nt) {
+        const int j = t / nu, r = t - j * nu;
+        inv[t] = (float)M[r * nu + j];
+    }
+    if (tid == 0) *ok = 1;
+}
+
+// Exact coarsest solve unless AGB_BOTTOM_EXACT=0 (read when an operator is created).
+bool use_exact_bottom()
+{
+    const char* s = getenv("AGB_BOTTOM_EXACT");
+    return !(s && s[0] == '0');
+}
+
+void launch_bottom_invert(cudaStream_t st, const LevelDesc& L, const double* A, float* inv, int* ok)
+{
+    const size_t nu = 3 * (size_t)L.count();
+    k_bottom_invert<<<1, 1024, nu * nu * sizeof(double), st>>>(L, A, inv, ok);
+    count_launch();
+}
 
 // Small bottom levels use the dense path unless AGB_BOTTOM_DENSE=0.
 bool use_dense_bottom()
@@ -586,12 +733,12 @@ void launch_bottom_assemble(cudaStream_t st, int sym, const LevelDesc& L, const 
 template <typename T>
 void launch_bottom_dense(cudaStream_t st, const LevelDesc& L, const double* A, const double* diag64, T* cor,
                          const T* res, int maxiter, double tol_rel, double tol_abs, int* ret_slot, int nub, int nuf,
-                         double omega)
+                         double omega, const float* inv, const int* inv_ok)
 {
     const size_t nu = 3 * (size_t)L.count();
     const size_t smem = (nu * nu + nu) * sizeof(T);
-    k_bottom_dense<T, T><<<1, DENSE_MAX, smem, st>>>(L, A, diag64, cor, res, maxiter, tol_rel, tol_abs, nub, nuf,
-                                                     omega, ret_slot);
+    pdl_launch(k_bottom_dense<T, T>, dim3(1), dim3(DENSE_MAX), smem, st, L, A, diag64, cor, res, maxiter, tol_rel,
+               tol_abs, nub, nuf, omega, ret_slot, inv, inv_ok);
     count_launch();
 }
 
@@ -600,12 +747,16 @@ void init_bottom_attributes()
     const int smem = (DENSE_MAX * DENSE_MAX + DENSE_MAX) * (int)sizeof(double);
     cudaFuncSetAttribute(k_bottom_dense<double, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     cudaFuncSetAttribute(k_bottom_dense<float, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_bottom_invert, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         DENSE_MAX * DENSE_MAX * (int)sizeof(double));
 }
 
 template void launch_bottom_dense<double>(cudaStream_t, const LevelDesc&, const double*, const double*, double*,
-                                          const double*, int, double, double, int*, int, int, double);
+                                          const double*, int, double, double, int*, int, int, double, const float*,
+                                          const int*);
 template void launch_bottom_dense<float>(cudaStream_t, const LevelDesc&, const double*, const double*, float*,
-                                         const float*, int, double, double, int*, int, int, double);
+                                         const float*, int, double, double, int*, int, int, double, const float*,
+                                         const int*);
 
 template <typename T>
 void launch_bottom(cudaStream_t st, int sym, const LevelDesc& L, const BCTable& bc, bool uniform, const double* ddw64,

@@ -19,6 +19,9 @@
 #include <cstdio>
 #include <cstdlib>
 
+#include <map>
+#include <mutex>
+
 #include "agb_internal.h"
 #include "stencil.cuh"
 
@@ -113,6 +116,7 @@ __global__ void __launch_bounds__(256) k_stencil_node(LevelDesc L, BCTable bc, G
                                                       const T* __restrict__ b, const T* __restrict__ dinv,
                                                       T* __restrict__ out, T omega, void* norm_slot, int shell)
 {
+    pdl_entry();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z * blockDim.z + threadIdx.z;
@@ -177,6 +181,7 @@ __global__ void __launch_bounds__(256) k_stencil_shell(LevelDesc L, BCTable bc, 
                                                        const T* __restrict__ dinv, T* __restrict__ out, T omega,
                                                        void* norm_slot)
 {
+    pdl_entry();
     const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     T nrm = 0;
     if (e < shell_count(L)) {
@@ -238,6 +243,7 @@ __global__ void __launch_bounds__(MT_X* MT_Y) k_stencil_march(LevelDesc L, Geo<T
                                                                  const T* __restrict__ dinv, T* __restrict__ out,
                                                                  T omega, void* norm_slot)
 {
+    pdl_entry();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     MarchSmem<T, SYM>& s = *reinterpret_cast<MarchSmem<T, SYM>*>(smem_raw);
     constexpr int NC = NCoef<SYM>::value;
@@ -385,6 +391,7 @@ __global__ void __launch_bounds__(MT_X* MT_Y) k_stencil_pipe(LevelDesc L, Geo<T>
                                                                 const T* __restrict__ b, const T* __restrict__ dinv,
                                                                 T* __restrict__ out, T omega, void* norm_slot)
 {
+    pdl_entry();
     extern __shared__ __align__(16) unsigned char smem_raw[];
     PipeSmem<T, SYM>& s = *reinterpret_cast<PipeSmem<T, SYM>*>(smem_raw);
     constexpr int NC = NCoef<SYM>::value;
@@ -477,7 +484,7 @@ __global__ void __launch_bounds__(MT_X* MT_Y) k_stencil_pipe(LevelDesc L, Geo<T>
 // diagonal
 // ---------------------------------------------------------------------------
 template <typename T, int SYM>
-__global__ void k_diagonal(LevelDesc L, BCTable bc, const T* __restrict__ ddw, T* __restrict__ diag)
+__global__ void k_diagonal(LevelDesc L, DiagGeo<T> dg, BCTable bc, const T* __restrict__ ddw, T* __restrict__ diag)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -492,7 +499,7 @@ __global__ void k_diagonal(LevelDesc L, BCTable bc, const T* __restrict__ ddw, T
     const long long p = L.idx(i, j, k);
     T c[NCoef<SYM>::value];
     for (int m = 0; m < NCoef<SYM>::value; m++) c[m] = ddw[m * L.S + p];
-    for (int q = 0; q < 3; q++) diag[q * L.S + p] = diag_entry<T, SYM>(c, L, bc, mn, mx, q);
+    for (int q = 0; q < 3; q++) diag[q * L.S + p] = diag_entry<T, SYM>(c, L, dg, bc, mn, mx, q);
 }
 
 // ---------------------------------------------------------------------------
@@ -524,6 +531,58 @@ bool use_pipe_kernel()
     return v;
 }
 
+// ---------------------------------------------------------------------------
+// side streams for the boundary shell
+// ---------------------------------------------------------------------------
+struct SideStream {
+    cudaStream_t st = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+};
+static std::mutex g_side_mutex;
+static std::map<cudaStream_t, SideStream> g_side;
+
+void register_side_stream(cudaStream_t main)
+{
+    const char* env = getenv("AGB_SHELL_OVERLAP");
+    if (!main || (env && env[0] == '0')) return;
+    SideStream sd;
+    if (cudaStreamCreateWithFlags(&sd.st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&sd.fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&sd.join, cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError();
+        if (sd.fork) cudaEventDestroy(sd.fork);
+        if (sd.st) cudaStreamDestroy(sd.st);
+        return;   // sweeps on this stream stay sequential
+    }
+    std::lock_guard<std::mutex> lock(g_side_mutex);
+    g_side[main] = sd;
+}
+
+void unregister_side_stream(cudaStream_t main)
+{
+    SideStream sd;
+    {
+        std::lock_guard<std::mutex> lock(g_side_mutex);
+        auto it = g_side.find(main);
+        if (it == g_side.end()) return;
+        sd = it->second;
+        g_side.erase(it);
+    }
+    cudaStreamSynchronize(sd.st);
+    cudaEventDestroy(sd.fork);
+    cudaEventDestroy(sd.join);
+    cudaStreamDestroy(sd.st);
+}
+
+static bool side_stream(cudaStream_t main, SideStream* out)
+{
+    std::lock_guard<std::mutex> lock(g_side_mutex);
+    auto it = g_side.find(main);
+    if (it == g_side.end()) return false;
+    *out = it->second;
+    return true;
+}
+
 template <typename T, int SYM, int MODE>
 static void stencil_dispatch(cudaStream_t st, const LevelDesc& L, const BCTable& bc, bool uniform, const T* ddw,
                              const T* x, const T* b, const T* diag, T* out, T omega, void* norm_slot)
@@ -534,7 +593,20 @@ static void stencil_dispatch(cudaStream_t st, const LevelDesc& L, const BCTable&
     const bool big = !L.per[0] && !L.per[1] && !L.per[2] && L.n[0] >= march_min_cells() &&
                      L.n[1] >= 16 && L.n[2] >= 16;
     if (big) {
-        // interior by the marching kernel, boundary shell by the per-node kernel
+        // interior by the marching kernel, boundary shell by the per-node
+        // kernel; with a side stream the shell is forked off first and joined
+        // after the interior, so the two overlap
+        SideStream sd;
+        const bool fork = side_stream(st, &sd);
+        const long long ns = shell_count(L);
+        if (fork) {
+            cudaEventRecord(sd.fork, st);
+            cudaStreamWaitEvent(sd.st, sd.fork, 0);
+            k_stencil_shell<T, SYM, MODE><<<(unsigned)((ns + 255) / 256), 256, 0, sd.st>>>(L, bc, g, ddw, x, b, diag,
+                                                                                       out, omega, norm_slot);
+            count_launch();
+            cudaEventRecord(sd.join, sd.st);
+        }
         dim3 blk(MT_X, MT_Y, 1);
         if (sizeof(T) == 4 && use_tma_kernel() && tma_supported(L) &&
             launch_stencil_tma(st, SYM, MODE, L, uniform, reinterpret_cast<const float*>(ddw),
@@ -545,24 +617,28 @@ static void stencil_dispatch(cudaStream_t st, const LevelDesc& L, const BCTable&
         } else if (sizeof(T) == 4 && use_pipe_kernel()) {
             const size_t smem = sizeof(PipeSmem<T, SYM>);
             dim3 grd((L.n[0] - 1 + MT_X - 1) / MT_X, (L.n[1] - 1 + MT_Y - 1) / MT_Y, (L.n[2] - 1 + PT_Z - 1) / PT_Z);
-            k_stencil_pipe<T, SYM, MODE><<<grd, blk, smem, st>>>(L, g, uniform ? 1 : 0, ddw, x, b, diag, out, omega,
-                                                                   norm_slot);
+            pdl_launch(k_stencil_pipe<T, SYM, MODE>, grd, blk, smem, st, L, g, uniform ? 1 : 0, ddw, x, b, diag, out,
+                       omega, norm_slot);
         } else {
             const size_t smem = sizeof(MarchSmem<T, SYM>);
             dim3 grd((L.n[0] - 1 + MT_X - 1) / MT_X, (L.n[1] - 1 + MT_Y - 1) / MT_Y, (L.n[2] - 1 + MT_Z - 1) / MT_Z);
-            k_stencil_march<T, SYM, MODE><<<grd, blk, smem, st>>>(L, g, uniform ? 1 : 0, ddw, x, b, diag, out, omega,
-                                                                    norm_slot);
+            pdl_launch(k_stencil_march<T, SYM, MODE>, grd, blk, smem, st, L, g, uniform ? 1 : 0, ddw, x, b, diag, out,
+                       omega, norm_slot);
         }
         count_launch();
-        const long long ns = shell_count(L);
-        k_stencil_shell<T, SYM, MODE><<<(unsigned)((ns + 255) / 256), 256, 0, st>>>(L, bc, g, ddw, x, b, diag, out,
-                                                                                    omega, norm_slot);
-        count_launch();
+        if (fork) {
+            cudaStreamWaitEvent(st, sd.join, 0);
+        } else {
+            pdl_launch(k_stencil_shell<T, SYM, MODE>, dim3((unsigned)((ns + 255) / 256)), dim3(256), 0, st, L, bc, g,
+                       ddw, x, b, diag, out, omega, norm_slot);
+            count_launch();
+        }
     } else {
         dim3 b2(32, 4, 2);
         if (L.nn[0] <= 16) b2 = dim3(8, 8, 4);
-        k_stencil_node<T, SYM, MODE><<<node_grid(L, b2), b2, 0, st>>>(L, bc, g, uniform ? 1 : 0, ddw, x, b, diag,
-                                                                       out, omega, norm_slot, 0); count_launch();
+        pdl_launch(k_stencil_node<T, SYM, MODE>, node_grid(L, b2), b2, 0, st, L, bc, g, uniform ? 1 : 0, ddw, x, b,
+                   diag, out, omega, norm_slot, 0);
+        count_launch();
     }
 }
 
@@ -612,8 +688,9 @@ template <typename T>
 void launch_diagonal(cudaStream_t st, int sym, const LevelDesc& L, const BCTable& bc, const T* ddw, T* diag)
 {
     dim3 blk(32, 4, 2);
-    if (sym == SYM_ISO) k_diagonal<T, SYM_ISO><<<node_grid(L, blk), blk, 0, st>>>(L, bc, ddw, diag);
-    else k_diagonal<T, SYM_MM><<<node_grid(L, blk), blk, 0, st>>>(L, bc, ddw, diag);
+    const DiagGeo<T> dg = make_diag_geo<T>(L);
+    if (sym == SYM_ISO) k_diagonal<T, SYM_ISO><<<node_grid(L, blk), blk, 0, st>>>(L, dg, bc, ddw, diag);
+    else k_diagonal<T, SYM_MM><<<node_grid(L, blk), blk, 0, st>>>(L, dg, bc, ddw, diag);
     count_launch();
 }
 

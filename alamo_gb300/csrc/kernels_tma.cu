@@ -84,6 +84,7 @@ __global__ void __launch_bounds__(TT_X* TT_Y) k_stencil_tma(LevelDesc L, Geo<flo
                                                             const float* __restrict__ dinv, float* __restrict__ out,
                                                             float omega, void* norm_slot, int* err, int kz)
 {
+    pdl_entry();
     typedef TmaLayout<SYM> Lay;
     constexpr int NC = Lay::NC;
     extern __shared__ __align__(128) unsigned char tsm_raw[];
@@ -314,8 +315,8 @@ static bool launch_tma_sm(cudaStream_t st, const LevelDesc& L, bool uniform, con
     int kz = TT_Z;
     while (kz > kz_min && (long long)cxy * ((L.n[2] - 1 + kz - 1) / kz) < 3LL * 2 * sm_count()) kz /= 2;
     dim3 grd((L.n[0] - 1 + TT_X - 1) / TT_X, (L.n[1] - 1 + TT_Y - 1) / TT_Y, (L.n[2] - 1 + kz - 1) / kz);
-    k_stencil_tma<SYM, MODE><<<grd, blk, TmaLayout<SYM>::SMEM, st>>>(L, g, uniform ? 1 : 0, mx, mc, ddw, b, dinv,
-                                                                     out, omega, norm_slot, err, kz);
+    pdl_launch(k_stencil_tma<SYM, MODE>, grd, blk, (size_t)TmaLayout<SYM>::SMEM, st, L, g, uniform ? 1 : 0, mx, mc, ddw,
+               b, dinv, out, omega, norm_slot, err, kz);
     return true;   // the caller counts the launch
 }
 

@@ -42,6 +42,7 @@ struct FineOffsets {
 template <typename T>
 __global__ void k_restrict(LevelDesc Lf, LevelDesc Lc, const T* __restrict__ fine, T* __restrict__ crse, int ncomp)
 {
+    pdl_entry();
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
     const int J = blockIdx.y * blockDim.y + threadIdx.y;
     const int K = blockIdx.z * blockDim.z + threadIdx.z;
@@ -73,6 +74,7 @@ template <> struct Pair<double> { typedef double2 type; };
 template <typename T>
 __global__ void k_interp(LevelDesc Lf, LevelDesc Lc, T* __restrict__ fine, const T* __restrict__ crse, int assign)
 {
+    pdl_entry();
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
     const int k = blockIdx.z * blockDim.z + threadIdx.z;
@@ -158,6 +160,7 @@ __global__ void k_convert(long long n, const TS* __restrict__ src, TD* __restric
 template <typename T>
 __global__ void k_axpy(long long n, T* __restrict__ y, const T* __restrict__ x, T a)
 {
+    pdl_entry();
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
         y[e] += a * x[e];
 }
@@ -173,6 +176,7 @@ template <> struct MaxSlot<float> {
 template <typename T>
 __global__ void k_norm_inf(long long n, const T* __restrict__ x, void* slot)
 {
+    pdl_entry();
     T m = 0;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
         const T a = fabs(x[e]);
@@ -253,6 +257,19 @@ __global__ void k_export(LevelDesc L, int ncomp, const TS* __restrict__ src, TD*
     }
 }
 
+// The first damped-Jacobi sweep from x = 0: A 0 = 0 in every row (interior,
+// displacement, traction and Neumann rows alike), so x + omega (b - A x) / D
+// is omega (b / D) node by node -- the sweep kernels' expression with x = 0,
+// equal to theirs up to the sign of a zero.
+template <typename T>
+__global__ void k_jacobi_zero(long long n, T* __restrict__ out, const T* __restrict__ b, const T* __restrict__ dinv,
+                              T omega)
+{
+    pdl_entry();
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
+        out[e] = omega * (b[e] * dinv[e]);
+}
+
 // y += a * x with x in FP32, y in FP64 (refinement accumulation)
 __global__ void k_axpy_mixed(long long n, double* __restrict__ y, const float* __restrict__ x, double a)
 {
@@ -280,6 +297,7 @@ __global__ void k_recip(long long n, const double* __restrict__ d, TD* __restric
 template <typename T>
 __global__ void k_mean3(LevelDesc L, T* __restrict__ x, double* __restrict__ sums, int subtract, void* norm_slot)
 {
+    pdl_entry();
     const long long cnt = L.count();
     double s[3] = {0, 0, 0};
     T m = 0;
@@ -339,7 +357,7 @@ template <typename T>
 void launch_restriction(cudaStream_t st, const LevelDesc& Lf, const LevelDesc& Lc, const T* fine, T* crse, int ncomp)
 {
     dim3 blk(32, 4, 2);
-    k_restrict<T><<<grid_for(Lc, blk), blk, 0, st>>>(Lf, Lc, fine, crse, ncomp); count_launch();
+    pdl_launch(k_restrict<T>, grid_for(Lc, blk), blk, 0, st, Lf, Lc, fine, crse, ncomp); count_launch();
 }
 
 template <typename T>
@@ -350,7 +368,7 @@ void launch_interpolation(cudaStream_t st, const LevelDesc& Lf, const LevelDesc&
     // one thread per fine pair (2I, 2I+1) of a row
     const dim3 grd(((Lf.nn[0] + 1) / 2 + blk.x - 1) / blk.x, (Lf.nn[1] + blk.y - 1) / blk.y,
                    (Lf.nn[2] + blk.z - 1) / blk.z);
-    k_interp<T><<<grd, blk, 0, st>>>(Lf, Lc, fine, crse, assign ? 1 : 0); count_launch();
+    pdl_launch(k_interp<T>, grd, blk, 0, st, Lf, Lc, fine, crse, assign ? 1 : 0); count_launch();
 }
 
 template <typename T>
@@ -371,7 +389,14 @@ template <typename T>
 void launch_axpy(cudaStream_t st, const LevelDesc& L, int ncomp, T* y, const T* x, T a)
 {
     const long long n = (long long)ncomp * L.S;
-    k_axpy<T><<<blocks_1d(n), 256, 0, st>>>(n, y, x, a); count_launch();
+    pdl_launch(k_axpy<T>, dim3(blocks_1d(n)), dim3(256), 0, st, n, y, x, a); count_launch();
+}
+
+template <typename T>
+void launch_jacobi_zero(cudaStream_t st, const LevelDesc& L, int ncomp, T* out, const T* b, const T* dinv, T omega)
+{
+    const long long n = (long long)ncomp * L.S;
+    pdl_launch(k_jacobi_zero<T>, dim3(blocks_1d(n)), dim3(256), 0, st, n, out, b, dinv, omega); count_launch();
 }
 
 template <typename T>
@@ -384,7 +409,7 @@ template <typename T>
 void launch_norm_inf(cudaStream_t st, const LevelDesc& L, int ncomp, const T* x, void* slot)
 {
     const long long n = (long long)ncomp * L.S;
-    k_norm_inf<T><<<blocks_1d(n), 256, 0, st>>>(n, x, slot); count_launch();
+    pdl_launch(k_norm_inf<T>, dim3(blocks_1d(n)), dim3(256), 0, st, n, x, slot); count_launch();
 }
 
 template <typename TD, typename TS>
@@ -419,9 +444,9 @@ void launch_remove_mean(cudaStream_t st, const LevelDesc& L, T* x, double* sums3
 {
     cudaMemsetAsync(sums3, 0, 3 * sizeof(double), st);
     const int g = blocks_1d(L.count());
-    k_mean3<T><<<g, 256, 0, st>>>(L, x, sums3, 0, nullptr);
+    pdl_launch(k_mean3<T>, dim3(g), dim3(256), 0, st, L, x, sums3, 0, (void*)nullptr);
     count_launch();
-    k_mean3<T><<<g, 256, 0, st>>>(L, x, sums3, 1, norm_slot);
+    pdl_launch(k_mean3<T>, dim3(g), dim3(256), 0, st, L, x, sums3, 1, norm_slot);
     count_launch();
 }
 
@@ -457,6 +482,7 @@ template <int K>
 __global__ void __launch_bounds__(256) k_multidot_w(long long n, const float* __restrict__ x, GcrVecs V,
                                                     const float* __restrict__ d, double* __restrict__ out)
 {
+    pdl_entry();
     float acc[K];
 #pragma unroll
     for (int i = 0; i < K; i++) acc[i] = 0;
@@ -488,6 +514,7 @@ template <int K>
 __global__ void k_gcr_orth(long long n, const double* __restrict__ beta, GcrVecs W, GcrVecs Z,
                            float* __restrict__ w, float* __restrict__ z)
 {
+    pdl_entry();
     float b[K];
 #pragma unroll
     for (int i = 0; i < K; i++) b[i] = (float)beta[i];
@@ -508,6 +535,7 @@ __global__ void k_gcr_orth(long long n, const double* __restrict__ beta, GcrVecs
 __global__ void k_gcr_step(long long n, const double* __restrict__ dots, float* __restrict__ w,
                            float* __restrict__ z, float* __restrict__ c, float* __restrict__ r, void* slot)
 {
+    pdl_entry();
     const double ww = dots[0], rw = dots[1];
     const float inv = ww > 0 ? (float)(1.0 / sqrt(ww)) : 0.0f;
     const float a = ww > 0 ? (float)(rw / sqrt(ww)) : 0.0f;   // coefficient of the unit direction
@@ -534,7 +562,7 @@ void launch_multidot_w(cudaStream_t st, long long n, int k, const float* x, cons
 {
     const int nb = blocks_1d(n);
     switch (k) {
-#define K_(K) case K: k_multidot_w<K><<<nb, 256, 0, st>>>(n, x, V, d, out); break;
+#define K_(K) case K: pdl_launch(k_multidot_w<K>, dim3(nb), dim3(256), 0, st, n, x, V, d, out); break;
         K_(1) K_(2) K_(3) K_(4) K_(5) K_(6) K_(7) K_(8) K_(9) K_(10) K_(11) K_(12) K_(13) K_(14) K_(15) K_(16)
 #undef K_
     default: return;
@@ -547,7 +575,7 @@ void launch_gcr_orth(cudaStream_t st, long long n, int k, const double* beta, co
 {
     const int nb = blocks_1d(n);
     switch (k) {
-#define K_(K) case K: k_gcr_orth<K><<<nb, 256, 0, st>>>(n, beta, W, Z, w, z); break;
+#define K_(K) case K: pdl_launch(k_gcr_orth<K>, dim3(nb), dim3(256), 0, st, n, beta, W, Z, w, z); break;
         K_(1) K_(2) K_(3) K_(4) K_(5) K_(6) K_(7) K_(8) K_(9) K_(10) K_(11) K_(12) K_(13) K_(14) K_(15) K_(16)
 #undef K_
     default: return;
@@ -558,7 +586,7 @@ void launch_gcr_orth(cudaStream_t st, long long n, int k, const double* beta, co
 void launch_gcr_step(cudaStream_t st, long long n, const double* dots, float* w, float* z, float* c, float* r,
                      void* slot)
 {
-    k_gcr_step<<<blocks_1d(n), 256, 0, st>>>(n, dots, w, z, c, r, slot);
+    pdl_launch(k_gcr_step, dim3(blocks_1d(n)), dim3(256), 0, st, n, dots, w, z, c, r, slot);
     count_launch();
 }
 
@@ -588,6 +616,7 @@ void launch_recip(cudaStream_t st, const LevelDesc& L, int ncomp, const double* 
     template void launch_average_ddw<T>(cudaStream_t, const LevelDesc&, const LevelDesc&, const T*, T*, int); \
     template void launch_axpy<T>(cudaStream_t, const LevelDesc&, int, T*, const T*, T);                      \
     template void launch_zero<T>(cudaStream_t, const LevelDesc&, int, T*);                                   \
+    template void launch_jacobi_zero<T>(cudaStream_t, const LevelDesc&, int, T*, const T*, const T*, T);     \
     template void launch_norm_inf<T>(cudaStream_t, const LevelDesc&, int, const T*, void*);                  \
     template void launch_recip<T>(cudaStream_t, const LevelDesc&, int, const double*, T*);                   \
     template void launch_remove_mean<T>(cudaStream_t, const LevelDesc&, T*, double*, void*);                 \

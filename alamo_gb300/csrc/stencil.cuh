@@ -319,10 +319,22 @@ __device__ __forceinline__ void boundary_row(const A& acc, const Geo<T>& g, cons
     bc_set<T>(bc.type[face], u, G, S, nrm, f);
 }
 
+// -2 / dx_d^2 in the arithmetic type, as the interior diagonal uses it
+// (evaluated once per launch or thread, not per entry: FP64 division is slow).
+template <typename T> struct DiagGeo {
+    T h2m[3];
+};
+template <typename T> __host__ __device__ inline DiagGeo<T> make_diag_geo(const LevelDesc& L)
+{
+    DiagGeo<T> dg;
+    for (int d = 0; d < 3; d++) dg.h2m[d] = (T)(-2.0 / L.dx[d] / L.dx[d]);
+    return dg;
+}
+
 // Diagonal of one component p at a node, Operator/Elastic.cpp:321-365.
 template <typename T, int SYM>
-__device__ __forceinline__ T diag_entry(const T* c, const LevelDesc& L, const BCTable& bc, const int mn[3],
-                                        const int mx[3], int p)
+__device__ __forceinline__ T diag_entry(const T* c, const LevelDesc& L, const DiagGeo<T>& dg, const BCTable& bc,
+                                        const int mn[3], const int mx[3], int p)
 {
     const bool bnd = mn[0] | mx[0] | mn[1] | mx[1] | mn[2] | mx[2];
     if (bnd) {
@@ -345,7 +357,7 @@ __device__ __forceinline__ T diag_entry(const T* c, const LevelDesc& L, const BC
     for (int a = 0; a < 3; a++)
         for (int b = 0; b < 3; b++)
             for (int d = 0; d < 3; d++) H[a][b][d] = 0;
-    for (int d = 0; d < 3; d++) H[p][d][d] = (T)(-2.0 / L.dx[d] / L.dx[d]);
+    for (int d = 0; d < 3; d++) H[p][d][d] = dg.h2m[d];
     T f[3];
     c_mul_m3<T, SYM>(c, H, f);
     return f[p];

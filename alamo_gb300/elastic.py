@@ -312,6 +312,13 @@ class Elastic:
         return ms.value
 
 
+def fp64_fma_peak(iters=600):
+    """Measured FP64 FMA throughput of the current device (TFLOP/s, launch ms)."""
+    tf, ms = ctypes.c_double(), ctypes.c_float()
+    check(lib().agb_fp64_fma_peak(int(iters), ctypes.byref(tf), ctypes.byref(ms)))
+    return tf.value, ms.value
+
+
 # ---------------------------------------------------------------------------
 # Solver::Nonlocal::Linear / Newton
 # ---------------------------------------------------------------------------

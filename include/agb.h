@@ -222,6 +222,13 @@ agb_status agb_batch_tuning(agb_batch b, int level, int dims[3]);
  * on the operator stream). */
 agb_status agb_op_time_sweep(agb_op op, int level, int precision, int mode, int reps, double* ms_per_launch);
 
+/* Measured FP64 fused-multiply-add throughput of the current device: one
+ * launch of 4 CTAs per SM, 256 threads, 8 independent FMA chains of
+ * 16 * iters steps per thread, timed with CUDA events on a private stream
+ * after one warm-up launch.  Writes TFLOP/s (an FMA counts 2) and, when ms is
+ * not NULL, the launch's time.  The FP64 stencils are bound by this pipe. */
+agb_status agb_fp64_fma_peak(int iters, double* tflops, float* ms);
+
 /* Pinned host memory (for callers that want asynchronous copies). */
 agb_status agb_host_alloc(size_t bytes, void** p);
 agb_status agb_host_free(void* p);

@@ -174,6 +174,34 @@ def test_mixed_gcr_solve(gpu_lib, problem, n):
     assert reps[8].iterations < reps[0].iterations
 
 
+@pytest.mark.parametrize("problem", [c1_problem, c2_problem])
+def test_mixed_exact_bottom(gpu_lib, monkeypatch, problem):
+    """The FP32 cycles' coarsest solve by the dense inverse (made once per
+    solve) against MLMG's BiCGStab bottom (AGB_BOTTOM_EXACT=0): both reach
+    1e-10 by the oracle's residual and agree with the FP64 oracle solve, and
+    the exact bottom takes at most one cycle more (a few cycles of a solve
+    that needs tens; each of its coarsest solves costs one product)."""
+    from alamo_gb300 import Linear
+    g, ddw, F0, b, rhs = problem(32)
+    xo, rep_o = O.solve(g, ddw, rhs, tol_rel=1e-10, tol_abs=0.0)
+    cycles = {}
+    for exact in ("1", "0"):
+        monkeypatch.setenv("AGB_BOTTOM_EXACT", exact)
+        op = gpu_op(g, ddw)
+        sol = Linear(op, precision=1, krylov=8)
+        x = np.zeros_like(rhs)
+        sol.solve(x, rhs, 1e-10, 0.0)
+        assert sol.report.status == 0
+        r = O.residual(g, ddw, x, rhs)
+        assert np.abs(r).max() <= 1e-10 * max(np.abs(rhs).max(), sol.report.res0) * 1.0000001
+        assert rel_err(x, xo) < 1e-6
+        cycles[exact] = sol.report.iterations
+        sol.Clear()
+        op.close()
+    print("cycles: exact bottom %d, BiCGStab bottom %d" % (cycles["1"], cycles["0"]))
+    assert cycles["1"] <= cycles["0"] + 1
+
+
 def test_mixed_gcr_rejects_bad_krylov(gpu_lib):
     from alamo_gb300 import AgbError, Linear
     g, ddw, F0, b, rhs = c1_problem(8)
