@@ -91,8 +91,9 @@ enum StencilMode { MODE_APPLY = 0, MODE_RESID = 1, MODE_JACOBI = 2 };
 // griddepcontrol.wait returns once the preceding grid has completed and its
 // writes are visible (so nothing the kernel reads or writes is touched
 // before), then launch_dependents lets the next kernel of the chain be
-// scheduled.  Launched without the attribute both are no-ops.  AGB_PDL=0
-// launches without it.
+// scheduled.  Launched without the attribute both are no-ops.  Off unless
+// AGB_PDL=1: on GB300 the 257^3 mixed solve measured 0.368 s with the
+// attribute and 0.337 s without it.
 __device__ __forceinline__ void pdl_entry()
 {
     asm volatile("griddepcontrol.wait;" ::: "memory");
@@ -103,8 +104,10 @@ bool pdl_enabled();
 // A side stream bound to an operator's stream: the boundary shell of a big
 // level's stencil sweep runs on it, forked from and joined back into the main
 // stream, so it overlaps the interior kernel (they write disjoint nodes).
-// Registered when the operator is created (outside any graph capture);
-// launches on an unregistered stream run the two kernels in order.
+// Registered when the operator is created (outside any graph capture) if
+// AGB_SHELL_OVERLAP=1; launches on an unregistered stream run the two kernels
+// in order (the default: on GB300 the overlap left the 257^3 solve unchanged
+// and slowed the finest-level sweep timed alone from 0.519 to 0.564 ms).
 void register_side_stream(cudaStream_t main);
 void unregister_side_stream(cudaStream_t main);
 template <typename... KArgs, typename... Args>
@@ -298,6 +301,38 @@ template <typename T>
 void launch_bottom(cudaStream_t st, int sym, const LevelDesc& L, const BCTable& bc, bool uniform,
                    const double* ddw64, const double* diag64, T* cor, const T* res, double* work, int maxiter,
                    double tol_rel, double tol_abs, int* ret_slot, int nub, int nuf, double omega);
+
+// The coarsest levels of an FP32 cycle in one CTA (kernels_tail.cu): levels
+// t .. bottom (at most TAIL_MAX_LEVELS, their moduli, 1/D and vectors in
+// shared memory), fcycle = 0 for MLMG::mgVcycle from level t (res_t ->
+// cor_t), 1 for the part of MLMG::mgFcycle below t.
+constexpr int TAIL_MAX_LEVELS = 4;
+constexpr size_t TAIL_SMEM_MAX = 200 * 1024;
+struct TailSpec {
+    int nlev;
+    LevelDesc levels[TAIL_MAX_LEVELS];
+    const float* ddw[TAIL_MAX_LEVELS];
+    const float* dinv[TAIL_MAX_LEVELS];
+    int uniform;
+    float omega;
+    int pre, post;
+    BCTable bc;
+    float* res_t;
+    float* cor_t;
+    const float* inv;      // exact bottom, used when *inv_ok
+    const int* inv_ok;
+    const double* A;       // dense bottom operator and the bottom level's FP64
+    const double* diag64;  // diagonal, global res / cor for the BiCGStab fallback
+    float* bres;
+    float* bcor;
+    int maxiter, nub, nuf;
+    double tol_rel, tol_abs;
+    int* ret_slot;
+};
+size_t coarse_tail_floats(const LevelDesc* lv, int nlev, int t, int nc);
+bool launch_coarse_tail(cudaStream_t st, int sym, const TailSpec& s, int fcycle);
+void init_tail_attributes();
+bool use_coarse_tail();
 
 void launch_newton_rhs(cudaStream_t st, int sym, const LevelDesc& L, const BCTable& bc, const double* ddw,
                        const double* F0, const double* u, const double* b, double* rhs, double* dw_work);

@@ -544,7 +544,7 @@ static std::map<cudaStream_t, SideStream> g_side;
 void register_side_stream(cudaStream_t main)
 {
     const char* env = getenv("AGB_SHELL_OVERLAP");
-    if (!main || (env && env[0] == '0')) return;
+    if (!main || !(env && env[0] == '1')) return;
     SideStream sd;
     if (cudaStreamCreateWithFlags(&sd.st, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&sd.fork, cudaEventDisableTiming) != cudaSuccess ||

@@ -58,6 +58,10 @@ def parse():
     ap.add_argument("--cycle", default="F", choices=["F", "V"])
     ap.add_argument("--krylov", type=int, default=8,
                     help="c2, rve: stored directions of the flexible GCR over the FP32 cycle (0: the FP32 cycles alone)")
+    ap.add_argument("--omega", type=float, default=-1.0,
+                    help="c2: Jacobi damping of the FP32 cycles (< 0: the operator's 2/3)")
+    ap.add_argument("--pre", type=int, default=2, help="c2: Fsmooth calls before restriction in the FP32 cycles")
+    ap.add_argument("--post", type=int, default=2, help="c2: Fsmooth calls after prolongation in the FP32 cycles")
     ap.add_argument("--workload", default="c2", choices=["c2", "rve", "learned", "sweep", "conv"],
                     help="c2: the 257^3 polycrystal (default); rve: batched periodic RVEs; learned: the learned "
                          "correction trained on 64^3 polycrystals and evaluated on the c2 system at 129^3 and 257^3; sweep: the finest-level "
@@ -215,7 +219,8 @@ def run_ours(args, dist):
     rhs_d = torch.from_numpy(rhs_h).cuda()
     sol_d = torch.zeros(3 * nodes, dtype=torch.float64, device="cuda")
     maxfmg = 100000000 if args.cycle == "F" else 0
-    mixed = Linear(op, precision=1, max_fmg_iter=maxfmg, krylov=args.krylov)
+    cyc = {"omega": args.omega, "pre_smooth": args.pre, "post_smooth": args.post}
+    mixed = Linear(op, precision=1, max_fmg_iter=maxfmg, krylov=args.krylov, **cyc)
 
     def one():
         sol_d.zero_()
@@ -255,7 +260,7 @@ def run_ours(args, dist):
         b_p = torch.from_numpy(b_h).pin_memory().numpy()
         u_t = torch.zeros(3 * nodes, dtype=torch.float64).pin_memory()
         u_p = u_t.numpy()
-        newton = Newton(op, precision=1, max_fmg_iter=maxfmg, krylov=args.krylov)
+        newton = Newton(op, precision=1, max_fmg_iter=maxfmg, krylov=args.krylov, **cyc)
 
         parts = []
 
@@ -301,7 +306,7 @@ def run_ours(args, dist):
 
     # plain FP64 multigrid of the same system, once
     if not args.no_plain:
-        plain = Linear(op, precision=0, max_fmg_iter=maxfmg)
+        plain = Linear(op, precision=0, max_fmg_iter=maxfmg, omega=2.0 / 3.0)   # MLMG's damping
         sol_d.zero_()
         plain.solve(sol_d, rhs_d, 1e-8, 0.0)
         pr = plain.report
