@@ -1091,7 +1091,6 @@ agb_status agb_op_create(const int n_cells[3], const double dx[3], const int per
     };
     if (cudaStreamCreateWithFlags(&op->st, cudaStreamNonBlocking) != cudaSuccess)
         return bail(fail(AGB_CUDA, "cudaStreamCreate failed"));
-    register_side_stream(op->st);
     cudaEventCreate(&op->e0);
     cudaEventCreate(&op->e1);
     if (!g_attr_done) {
@@ -1170,10 +1169,7 @@ agb_status agb_op_destroy(agb_op op)
     if (op->h_slots) cudaFreeHost(op->h_slots);
     if (op->e0) cudaEventDestroy(op->e0);
     if (op->e1) cudaEventDestroy(op->e1);
-    if (op->st) {
-        unregister_side_stream(op->st);
-        cudaStreamDestroy(op->st);
-    }
+    if (op->st) cudaStreamDestroy(op->st);
     delete op;
     return AGB_OK;
 }

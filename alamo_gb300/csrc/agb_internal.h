@@ -101,15 +101,6 @@ __device__ __forceinline__ void pdl_entry()
 }
 bool pdl_enabled();
 
-// A side stream bound to an operator's stream: the boundary shell of a big
-// level's stencil sweep runs on it, forked from and joined back into the main
-// stream, so it overlaps the interior kernel (they write disjoint nodes).
-// Registered when the operator is created (outside any graph capture) if
-// AGB_SHELL_OVERLAP=1; launches on an unregistered stream run the two kernels
-// in order (the default: on GB300 the overlap left the 257^3 solve unchanged
-// and slowed the finest-level sweep timed alone from 0.519 to 0.564 ms).
-void register_side_stream(cudaStream_t main);
-void unregister_side_stream(cudaStream_t main);
 template <typename... KArgs, typename... Args>
 inline void pdl_launch(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, Args... args)
 {
@@ -274,11 +265,13 @@ void launch_remove_mean(cudaStream_t st, const LevelDesc& L, T* x, double* sums3
 template <typename TD>
 void launch_recip(cudaStream_t st, const LevelDesc& L, int ncomp, const double* d, TD* r);
 void init_kernel_attributes();
-// FP32 interior sweep with TMA plane copies (kernels_tma.cu); false = not launched
+// FP32 interior sweep with TMA plane copies, and the x-face boundary rows of
+// the interior's y and z range (kernels_tma.cu); false = not launched
 bool use_tma_kernel();
 bool tma_supported(const LevelDesc& L);
-bool launch_stencil_tma(cudaStream_t st, int sym, int mode, const LevelDesc& L, bool uniform, const float* ddw,
-                        const float* x, const float* b, const float* dinv, float* out, float omega, void* norm_slot);
+bool launch_stencil_tma(cudaStream_t st, int sym, int mode, const LevelDesc& L, const BCTable& bc, bool uniform,
+                        const float* ddw, const float* x, const float* b, const float* dinv, float* out, float omega,
+                        void* norm_slot);
 int tma_error_take();   // 1 if a TMA kernel's bounded wait ran out since the last call
 void init_tma_attributes();
 

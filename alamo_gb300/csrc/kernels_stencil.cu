@@ -19,9 +19,6 @@
 #include <cstdio>
 #include <cstdlib>
 
-#include <map>
-#include <mutex>
-
 #include "agb_internal.h"
 #include "stencil.cuh"
 
@@ -146,13 +143,15 @@ __global__ void __launch_bounds__(256) k_stencil_node(LevelDesc L, BCTable bc, G
 // boundary shell of a box with no periodic direction: one thread per boundary
 // node, enumerated plane k=0, plane k=n2, then the rings of the planes between
 // ---------------------------------------------------------------------------
-__host__ __device__ inline long long shell_count(const LevelDesc& L)
+// (with xf = 0 the x-face nodes between the y rows are left out: the TMA
+// interior kernel computes them)
+__host__ __device__ inline long long shell_count(const LevelDesc& L, int xf)
 {
     const long long a = (long long)L.nn[0] * L.nn[1];
-    return 2 * a + (long long)(L.nn[2] - 2) * (2LL * L.nn[0] + 2LL * (L.nn[1] - 2));
+    return 2 * a + (long long)(L.nn[2] - 2) * (2LL * L.nn[0] + (xf ? 2LL * (L.nn[1] - 2) : 0LL));
 }
 
-__device__ __forceinline__ void shell_node(const LevelDesc& L, long long e, int& i, int& j, int& k)
+__device__ __forceinline__ void shell_node(const LevelDesc& L, long long e, int xf, int& i, int& j, int& k)
 {
     const long long a = (long long)L.nn[0] * L.nn[1];
     if (e < 2 * a) {
@@ -162,7 +161,7 @@ __device__ __forceinline__ void shell_node(const LevelDesc& L, long long e, int&
         i = (int)(r % L.nn[0]);
         return;
     }
-    const long long e2 = e - 2 * a, pm = 2LL * L.nn[0] + 2LL * (L.nn[1] - 2);
+    const long long e2 = e - 2 * a, pm = 2LL * L.nn[0] + (xf ? 2LL * (L.nn[1] - 2) : 0LL);
     k = 1 + (int)(e2 / pm);
     const int r = (int)(e2 % pm);
     if (r < 2 * L.nn[0]) {
@@ -179,14 +178,14 @@ template <typename T, int SYM, int MODE>
 __global__ void __launch_bounds__(256) k_stencil_shell(LevelDesc L, BCTable bc, Geo<T> g, const T* __restrict__ ddw,
                                                        const T* __restrict__ x, const T* __restrict__ b,
                                                        const T* __restrict__ dinv, T* __restrict__ out, T omega,
-                                                       void* norm_slot)
+                                                       void* norm_slot, int xf)
 {
     pdl_entry();
     const long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     T nrm = 0;
-    if (e < shell_count(L)) {
+    if (e < shell_count(L, xf)) {
         int i, j, k;
-        shell_node(L, e, i, j, k);
+        shell_node(L, e, xf, i, j, k);
         const int pos[3] = {i, j, k};
         int mn[3], mx[3];
 #pragma unroll
@@ -531,58 +530,6 @@ bool use_pipe_kernel()
     return v;
 }
 
-// ---------------------------------------------------------------------------
-// side streams for the boundary shell
-// ---------------------------------------------------------------------------
-struct SideStream {
-    cudaStream_t st = nullptr;
-    cudaEvent_t fork = nullptr, join = nullptr;
-};
-static std::mutex g_side_mutex;
-static std::map<cudaStream_t, SideStream> g_side;
-
-void register_side_stream(cudaStream_t main)
-{
-    const char* env = getenv("AGB_SHELL_OVERLAP");
-    if (!main || !(env && env[0] == '1')) return;
-    SideStream sd;
-    if (cudaStreamCreateWithFlags(&sd.st, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&sd.fork, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&sd.join, cudaEventDisableTiming) != cudaSuccess) {
-        cudaGetLastError();
-        if (sd.fork) cudaEventDestroy(sd.fork);
-        if (sd.st) cudaStreamDestroy(sd.st);
-        return;   // sweeps on this stream stay sequential
-    }
-    std::lock_guard<std::mutex> lock(g_side_mutex);
-    g_side[main] = sd;
-}
-
-void unregister_side_stream(cudaStream_t main)
-{
-    SideStream sd;
-    {
-        std::lock_guard<std::mutex> lock(g_side_mutex);
-        auto it = g_side.find(main);
-        if (it == g_side.end()) return;
-        sd = it->second;
-        g_side.erase(it);
-    }
-    cudaStreamSynchronize(sd.st);
-    cudaEventDestroy(sd.fork);
-    cudaEventDestroy(sd.join);
-    cudaStreamDestroy(sd.st);
-}
-
-static bool side_stream(cudaStream_t main, SideStream* out)
-{
-    std::lock_guard<std::mutex> lock(g_side_mutex);
-    auto it = g_side.find(main);
-    if (it == g_side.end()) return false;
-    *out = it->second;
-    return true;
-}
-
 template <typename T, int SYM, int MODE>
 static void stencil_dispatch(cudaStream_t st, const LevelDesc& L, const BCTable& bc, bool uniform, const T* ddw,
                              const T* x, const T* b, const T* diag, T* out, T omega, void* norm_slot)
@@ -594,26 +541,15 @@ static void stencil_dispatch(cudaStream_t st, const LevelDesc& L, const BCTable&
                      L.n[1] >= 16 && L.n[2] >= 16;
     if (big) {
         // interior by the marching kernel, boundary shell by the per-node
-        // kernel; with a side stream the shell is forked off first and joined
-        // after the interior, so the two overlap
-        SideStream sd;
-        const bool fork = side_stream(st, &sd);
-        const long long ns = shell_count(L);
-        if (fork) {
-            cudaEventRecord(sd.fork, st);
-            cudaStreamWaitEvent(sd.st, sd.fork, 0);
-            k_stencil_shell<T, SYM, MODE><<<(unsigned)((ns + 255) / 256), 256, 0, sd.st>>>(L, bc, g, ddw, x, b, diag,
-                                                                                       out, omega, norm_slot);
-            count_launch();
-            cudaEventRecord(sd.join, sd.st);
-        }
+        // kernel (the TMA kernel also takes the x-face nodes)
         dim3 blk(MT_X, MT_Y, 1);
+        bool tma = false;
         if (sizeof(T) == 4 && use_tma_kernel() && tma_supported(L) &&
-            launch_stencil_tma(st, SYM, MODE, L, uniform, reinterpret_cast<const float*>(ddw),
+            launch_stencil_tma(st, SYM, MODE, L, bc, uniform, reinterpret_cast<const float*>(ddw),
                                reinterpret_cast<const float*>(x), reinterpret_cast<const float*>(b),
                                reinterpret_cast<const float*>(diag), reinterpret_cast<float*>(out), (float)omega,
                                norm_slot)) {
-            // launched by launch_stencil_tma
+            tma = true;   // launched by launch_stencil_tma
         } else if (sizeof(T) == 4 && use_pipe_kernel()) {
             const size_t smem = sizeof(PipeSmem<T, SYM>);
             dim3 grd((L.n[0] - 1 + MT_X - 1) / MT_X, (L.n[1] - 1 + MT_Y - 1) / MT_Y, (L.n[2] - 1 + PT_Z - 1) / PT_Z);
@@ -626,13 +562,11 @@ static void stencil_dispatch(cudaStream_t st, const LevelDesc& L, const BCTable&
                        omega, norm_slot);
         }
         count_launch();
-        if (fork) {
-            cudaStreamWaitEvent(st, sd.join, 0);
-        } else {
-            pdl_launch(k_stencil_shell<T, SYM, MODE>, dim3((unsigned)((ns + 255) / 256)), dim3(256), 0, st, L, bc, g,
-                       ddw, x, b, diag, out, omega, norm_slot);
-            count_launch();
-        }
+        const int xf = tma ? 0 : 1;
+        const long long ns = shell_count(L, xf);
+        pdl_launch(k_stencil_shell<T, SYM, MODE>, dim3((unsigned)((ns + 255) / 256)), dim3(256), 0, st, L, bc, g, ddw,
+                   x, b, diag, out, omega, norm_slot, xf);
+        count_launch();
     } else {
         dim3 b2(32, 4, 2);
         if (L.nn[0] <= 16) b2 = dim3(8, 8, 4);

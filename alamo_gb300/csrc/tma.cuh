@@ -22,6 +22,13 @@ __device__ __forceinline__ void mbar_expect(uint32_t bar, uint32_t bytes)
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
 }
 
+// One arrival (release semantics at CTA scope) on a barrier initialised with
+// the number of arriving threads.
+__device__ __forceinline__ void mbar_arrive(uint32_t bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
 // Bounded wait for the phase of parity `parity` to complete: false after
 // about 2^31 clock cycles (~1 s at 2 GHz) without completion.
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
