@@ -123,7 +123,6 @@ struct agb_op_s {
     double* bottom_A = nullptr;   // dense coarsest-level operator (small bottom levels)
     float* bottom_inv32 = nullptr;   // its inverse for the FP32 cycles (exact coarsest solve)
     int* bottom_inv_ok = nullptr;    // device flag: the inverse exists
-    int tail_level = -1;             // FP32 cycles: levels from here down run in one CTA (kernels_tail.cu)
     int* d_ret = nullptr;
     char* stage = nullptr;       // bounded staging buffer for pageable host copies
     size_t stage_bytes = 0;
@@ -533,58 +532,18 @@ template <typename T> struct Engine {
                          op->bottom_work, p.bottom_max_iter, p.bottom_tol_rel, p.bottom_tol_abs, op->d_ret,
                          p.bottom_smooth, p.final_smooth, op->omega);
     }
-    // First level of the coarse tail for these cycles, or -1: FP32 cycles only
-    // (the FP64 cycles keep MLMG's launch sequence and BiCGStab bottom).
-    int tail() const { return (sizeof(T) == 4 && op->f32_ready) ? op->tail_level : -1; }
-    // Levels tail() .. bottom in one CTA: fcycle = 0 for the V-cycle from
-    // there (res -> cor of the tail level), 1 for the F-cycle's part below it.
-    void run_tail(int fcycle)
-    {
-        const int t = tail(), b = bot();
-        TailSpec ts;
-        ts.nlev = b - t + 1;
-        for (int m = 0; m < ts.nlev; m++) {
-            Level& v = lv(t + m);
-            ts.levels[m] = v.L;
-            ts.ddw[m] = (const float*)A::ddw(v);
-            ts.dinv[m] = (const float*)A::dinv(v);
-        }
-        ts.uniform = op->uniform ? 1 : 0;
-        ts.omega = (float)op->omega;
-        ts.pre = p.pre_smooth;
-        ts.post = p.post_smooth;
-        ts.bc = op->bc;
-        ts.res_t = (float*)A::res(lv(t));
-        ts.cor_t = (float*)A::cor(lv(t));
-        ts.inv = op->bottom_inv32;
-        ts.inv_ok = op->bottom_inv_ok;
-        ts.A = op->bottom_A;
-        ts.diag64 = lv(b).diag64;
-        ts.bres = lv(b).res32;
-        ts.bcor = lv(b).cor32;
-        ts.maxiter = p.bottom_max_iter;
-        ts.nub = p.bottom_smooth;
-        ts.nuf = p.final_smooth;
-        ts.tol_rel = p.bottom_tol_rel;
-        ts.tol_abs = p.bottom_tol_abs;
-        ts.ret_slot = op->d_ret;
-        launch_coarse_tail(op->st, op->sym, ts, fcycle);
-    }
     // MLMG::mgVcycle(amrlev = 0, mglev_top)
     void vcycle(int top)
     {
         const int b = bot();
-        const int t = (tail() > top) ? tail() : -1;   // the tail takes the levels from t down
-        const int last = t >= 0 ? t : b;
-        for (int l = top; l < last; l++) {
+        for (int l = top; l < b; l++) {
             Level& v = lv(l);
             smooth_from_zero(l, A::cor(v), A::res(v), p.pre_smooth);
             residual(l, A::cor(v), A::res(v), A::rescor(v), nullptr);
             launch_restriction<T>(op->st, v.L, lv(l + 1).L, A::rescor(v), A::res(lv(l + 1)), 3);
         }
-        if (t >= 0) run_tail(0);
-        else bottom();
-        for (int l = last - 1; l >= top; l--) {
+        bottom();
+        for (int l = b - 1; l >= top; l--) {
             Level& v = lv(l);
             launch_interpolation<T>(op->st, v.L, lv(l + 1).L, A::cor(v), A::cor(lv(l + 1)), false);
             smooth(l, A::cor(v), A::res(v), p.post_smooth);
@@ -594,13 +553,10 @@ template <typename T> struct Engine {
     void fcycle()
     {
         const int b = bot();
-        const int t = tail() > 0 ? tail() : -1;
-        const int last = t >= 0 ? t : b;
-        for (int l = 1; l <= last; l++)
+        for (int l = 1; l <= b; l++)
             launch_restriction<T>(op->st, lv(l - 1).L, lv(l).L, A::res(lv(l - 1)), A::res(lv(l)), 3);
-        if (t >= 0) run_tail(1);
-        else bottom();
-        for (int l = last - 1; l >= 0; l--) {
+        bottom();
+        for (int l = b - 1; l >= 0; l--) {
             Level& v = lv(l);
             launch_interpolation<T>(op->st, v.L, lv(l + 1).L, A::cor(v), A::cor(lv(l + 1)), true);
             residual(l, A::cor(v), A::res(v), A::rescor(v), nullptr);
@@ -1097,7 +1053,6 @@ agb_status agb_op_create(const int n_cells[3], const double dx[3], const int per
         init_kernel_attributes();
         init_bottom_attributes();
         init_tma_attributes();
-        init_tail_attributes();
         g_attr_done = true;
     }
     int dev = 0;
@@ -1139,17 +1094,6 @@ agb_status agb_op_create(const int n_cells[3], const double dx[3], const int per
                 return bail(s);
             if ((s = op->alloc(&op->bottom_inv_ok, 1)) != AGB_OK) return bail(s);
         }
-    }
-    // the coarse tail: the most levels (at least two, ending at the dense
-    // bottom) whose data fit one CTA's shared memory, unless AGB_TAIL=0
-    if (op->bottom_inv32 && use_coarse_tail()) {
-        std::vector<LevelDesc> ls;
-        for (auto& lv : op->lev) ls.push_back(lv.L);
-        for (int t = 1; t < (int)ls.size(); t++)
-            if (coarse_tail_floats(ls.data(), (int)ls.size(), t, op->nc) > 0) {
-                op->tail_level = t;
-                break;
-            }
     }
     op->stage_bytes = 64u << 20;
     if ((s = op->alloc(&op->stage, op->stage_bytes)) != AGB_OK) return bail(s);

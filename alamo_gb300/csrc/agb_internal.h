@@ -295,38 +295,6 @@ void launch_bottom(cudaStream_t st, int sym, const LevelDesc& L, const BCTable& 
                    const double* ddw64, const double* diag64, T* cor, const T* res, double* work, int maxiter,
                    double tol_rel, double tol_abs, int* ret_slot, int nub, int nuf, double omega);
 
-// The coarsest levels of an FP32 cycle in one CTA (kernels_tail.cu): levels
-// t .. bottom (at most TAIL_MAX_LEVELS, their moduli, 1/D and vectors in
-// shared memory), fcycle = 0 for MLMG::mgVcycle from level t (res_t ->
-// cor_t), 1 for the part of MLMG::mgFcycle below t.
-constexpr int TAIL_MAX_LEVELS = 4;
-constexpr size_t TAIL_SMEM_MAX = 200 * 1024;
-struct TailSpec {
-    int nlev;
-    LevelDesc levels[TAIL_MAX_LEVELS];
-    const float* ddw[TAIL_MAX_LEVELS];
-    const float* dinv[TAIL_MAX_LEVELS];
-    int uniform;
-    float omega;
-    int pre, post;
-    BCTable bc;
-    float* res_t;
-    float* cor_t;
-    const float* inv;      // exact bottom, used when *inv_ok
-    const int* inv_ok;
-    const double* A;       // dense bottom operator and the bottom level's FP64
-    const double* diag64;  // diagonal, global res / cor for the BiCGStab fallback
-    float* bres;
-    float* bcor;
-    int maxiter, nub, nuf;
-    double tol_rel, tol_abs;
-    int* ret_slot;
-};
-size_t coarse_tail_floats(const LevelDesc* lv, int nlev, int t, int nc);
-bool launch_coarse_tail(cudaStream_t st, int sym, const TailSpec& s, int fcycle);
-void init_tail_attributes();
-bool use_coarse_tail();
-
 void launch_newton_rhs(cudaStream_t st, int sym, const LevelDesc& L, const BCTable& bc, const double* ddw,
                        const double* F0, const double* u, const double* b, double* rhs, double* dw_work);
 void launch_stress(cudaStream_t st, int sym, const LevelDesc& L, const double* ddw, const double* F0,

@@ -1,5 +1,5 @@
-// bottom.cuh -- the dense coarsest-level BiCGStab of one CTA, shared by the
-// bottom kernels and the coarse-tail kernel.
+// bottom.cuh -- the dense coarsest-level BiCGStab of one CTA (the dense
+// bottom kernel's body), with its block reductions.
 #pragma once
 #include "agb_internal.h"
 #include "stencil.cuh"

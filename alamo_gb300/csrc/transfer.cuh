@@ -1,5 +1,5 @@
 // transfer.cuh -- per-node arithmetic of the inter-level transfers, shared
-// by the single-box, batched and coarse-tail kernels.
+// by the single-box and batched kernels.
 //
 //   restriction     Operator<Node>::restriction, Operator/Operator.cpp:262-363
 //   prolongation    Operator<Node>::interpolation, Operator.cpp:365-434

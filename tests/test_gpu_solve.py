@@ -202,36 +202,6 @@ def test_mixed_exact_bottom(gpu_lib, monkeypatch, problem):
     assert cycles["1"] <= cycles["0"] + 1
 
 
-@pytest.mark.parametrize("problem,fmg", [(c1_problem, True), (c2_problem, True), (c2_problem, False)])
-def test_mixed_coarse_tail(gpu_lib, monkeypatch, problem, fmg):
-    """The FP32 cycles' coarsest levels (9^3, 5^3, 3^3 nodes of a 32^3-cell
-    box) run in one CTA (the coarse tail) against the launch-per-step cycle
-    (AGB_TAIL=0), in F- and V-cycles: both reach 1e-10 by the oracle's
-    residual, agree with the FP64 oracle solve, and take the same number of
-    cycles within one."""
-    from alamo_gb300 import Linear
-    g, ddw, F0, b, rhs = problem(32)
-    xo, rep_o = O.solve(g, ddw, rhs, tol_rel=1e-10, tol_abs=0.0)
-    kw = {} if fmg else {"max_fmg_iter": 0}
-    cycles, sols = {}, {}
-    for tail in ("1", "0"):   # AGB_TAIL=1 turns the coarse tail on (it is off by default)
-        monkeypatch.setenv("AGB_TAIL", tail)
-        op = gpu_op(g, ddw)
-        sol = Linear(op, precision=1, krylov=8, **kw)
-        x = np.zeros_like(rhs)
-        sol.solve(x, rhs, 1e-10, 0.0)
-        assert sol.report.status == 0
-        r = O.residual(g, ddw, x, rhs)
-        assert np.abs(r).max() <= 1e-10 * max(np.abs(rhs).max(), sol.report.res0) * 1.0000001
-        assert rel_err(x, xo) < 1e-6
-        cycles[tail], sols[tail] = sol.report.iterations, x
-        sol.Clear()
-        op.close()
-    print("cycles: coarse tail %d, launch per step %d" % (cycles["1"], cycles["0"]))
-    assert abs(cycles["1"] - cycles["0"]) <= 1
-    assert rel_err(sols["1"], sols["0"]) < 1e-8
-
-
 def test_mixed_gcr_rejects_bad_krylov(gpu_lib):
     from alamo_gb300 import AgbError, Linear
     g, ddw, F0, b, rhs = c1_problem(8)
