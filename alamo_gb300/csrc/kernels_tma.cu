@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(TT_X* TMA_WARPS, 2)
             for (int m = 0; m < NC; m++) acc.cm[m] = __ldg(ddw + m * S + p);
         }
         int waited = 0;     // fills known complete
-        // b and 1/D of the first plane; later planes are fetched one plane ahead
+        // b and 1/D of the first two planes; later planes are fetched two planes ahead
         float bq[3] = {0, 0, 0}, dq[3] = {0, 0, 0};
         auto fetch = [&](int k, float* bb, float* dd) {
             if (!mine || k >= k1) return;
@@ -178,12 +178,14 @@ __global__ void __launch_bounds__(TT_X* TMA_WARPS, 2)
 #pragma unroll
                 for (int c = 0; c < 3; c++) dd[c] = __ldg(dinv + c * S + q);
         };
+        float bn[3] = {0, 0, 0}, dn[3] = {0, 0, 0};
         fetch(k0, bq, dq);
+        fetch(k0 + 1, bn, dn);
         for (int k = k0; k < k1; k++) {
             const int it = k - k0;
             const long long q = mine ? L.idx(i, j, k) : 0;
-            float bn[3] = {0, 0, 0}, dn[3] = {0, 0, 0};
-            fetch(k + 1, bn, dn);
+            float bnn[3] = {0, 0, 0}, dnn[3] = {0, 0, 0};
+            fetch(k + 2, bnn, dnn);
             // planes k-1, k, k+1 = fills it, it+1, it+2
             bool good = true;
             for (int f = waited; f <= it + 2 && good; f++)
@@ -251,6 +253,8 @@ __global__ void __launch_bounds__(TT_X* TMA_WARPS, 2)
             for (int c = 0; c < 3; c++) {
                 bq[c] = bn[c];
                 dq[c] = dn[c];
+                bn[c] = bnn[c];
+                dn[c] = dnn[c];
             }
             // this warp is done with the u slot of plane k-1 and the moduli
             // slot of plane k: release them for fill it+4
