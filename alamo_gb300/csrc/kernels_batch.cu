@@ -70,6 +70,7 @@ template <typename T> __device__ __forceinline__ Geo<T> geo_of(const BProb& p)
         g.h2[d] = (T)p.h2[d];
         g.hm[d] = (T)p.hm[d];
     }
+    g.cube = 0;   // the batched kernels keep the general row form
     return g;
 }
 
