@@ -37,9 +37,9 @@ namespace agb {
 
 namespace {
 
-constexpr int TT_X = 32, TT_Y = 5, TT_Z = 32;      // tile and the longest k-chunk
+constexpr int TT_X = 32, TT_Y = 8, TT_Z = 32;      // tile and the longest k-chunk
 constexpr int TH_Y = TT_Y + 2, TW = 36;             // halo rows, halo row width (9 x 16 bytes)
-constexpr int TU = 5, TC = 4;                       // ring depths
+constexpr int TU = 4, TC = 3;                       // ring depths
 
 template <int NCOMP> struct SlotSize {
     // floats per slot, padded so every slot starts on a 128-byte boundary
@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(TT_X* TMA_WARPS, 2)
     const bool mine = ty < TT_Y && (i < L.n[0]) && (j < L.n[1]);
     // face warp: lane -> (side, row); the node (fi, fj, k) sits at column fcol of the halo box
     const int fside = tx >> 3, frow = tx & 7;
-    const bool fmine = face_warp && tx < 16 && frow < TT_Y && j0 + frow < L.n[1] &&
+    const bool fmine = face_warp && tx < 16 && j0 + frow < L.n[1] &&
                        (fside == 0 ? blockIdx.x == 0 : blockIdx.x == gridDim.x - 1);
     const int fi = fside == 0 ? 0 : L.n[0];
     const int fcol = fi - (i0 - 1);
