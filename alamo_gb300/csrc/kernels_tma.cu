@@ -37,7 +37,7 @@ namespace agb {
 
 namespace {
 
-constexpr int TT_X = 32, TT_Y = 8, TT_Z = 32;      // tile and the longest k-chunk
+constexpr int TT_X = 32, TT_Y = 8, TT_Z = 16;      // tile and the default longest k-chunk
 constexpr int TH_Y = TT_Y + 2, TW = 36;             // halo rows, halo row width (9 x 16 bytes)
 constexpr int TU = 4, TC = 3;                       // ring depths
 
@@ -360,16 +360,21 @@ static bool launch_tma_sm(cudaStream_t st, const LevelDesc& L, const BCTable& bc
     if (!err) return false;
     const Geo<float> g = make_geo<float>(L);
     dim3 blk(TT_X, TMA_WARPS, 1);
-    // k-chunk: the longest (least halo re-read) that still gives at least
-    // three waves of 2 CTAs on each SM, and no shorter than 4
-    // planes (AGB_TMA_KZ_MIN)
+    // k-chunk: the longest (least halo re-read) up to TT_Z planes
+    // (AGB_TMA_KZ_MAX) that still gives at least three waves of 2 CTAs on
+    // each SM, and no shorter than 4 planes (AGB_TMA_KZ_MIN)
     const int cxy = ((L.n[0] - 1 + TT_X - 1) / TT_X) * ((L.n[1] - 1 + TT_Y - 1) / TT_Y);
+    static const int kz_max = [] {
+        const char* e = getenv("AGB_TMA_KZ_MAX");
+        const int v = e ? atoi(e) : TT_Z;
+        return v >= 1 && v <= 256 ? v : TT_Z;
+    }();
     static const int kz_min = [] {
         const char* e = getenv("AGB_TMA_KZ_MIN");
         const int v = e ? atoi(e) : 4;
-        return v >= 1 && v <= TT_Z ? v : 4;
+        return v >= 1 && v <= kz_max ? v : 4;
     }();
-    int kz = TT_Z;
+    int kz = kz_max;
     while (kz > kz_min && (long long)cxy * ((L.n[2] - 1 + kz - 1) / kz) < 3LL * 2 * sm_count()) kz /= 2;
     dim3 grd((L.n[0] - 1 + TT_X - 1) / TT_X, (L.n[1] - 1 + TT_Y - 1) / TT_Y, (L.n[2] - 1 + kz - 1) / kz);
     pdl_launch(k_stencil_tma<SYM, MODE>, grd, blk, (size_t)TmaLayout<SYM>::SMEM, st, L, g, uniform ? 1 : 0, mx, mc, ddw,

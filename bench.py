@@ -37,10 +37,11 @@ WORKLOAD = ("257^3-node cubic Voronoi polycrystal (64 grains, C11/C12/C44 = 1.68
             "uniaxial tension u_x=0.01, solve to 1e-8 relative FP64 residual")
 BYTES_PER_NODE = {"jacobi_f32_cubic": 132, "fapply_f32_cubic": 108, "jacobi_f64_cubic": 264,
                   "fapply_f64_cubic": 216}
-# FP64 operations of one interior node of the damped-Jacobi sweep (an FMA
-# counts 2), counted by ncu on the marching kernel (DFMA, DADD, DMUL thread
-# instructions over the interior nodes of one launch)
-FLOPS_PER_NODE = {"jacobi_f64_cubic": 372}
+# FP64 operations of one interior node of the damped-Jacobi sweep on cubic
+# cells (an FMA counts 2), counted by ncu on the marching kernel (DFMA, DADD,
+# DMUL thread instructions over the interior nodes of one 65^3 launch:
+# 98 + 129 + 26)
+FLOPS_PER_NODE = {"jacobi_f64_cubic": 351}
 
 
 def parse():
