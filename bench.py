@@ -299,7 +299,8 @@ def run_ours(args, dist):
     ms_j32 = op.time_sweep(0, "f32", 2, 20)
     ms_a32 = op.time_sweep(0, "f32", 0, 20)
     ms_j64 = op.time_sweep(0, "f64", 2, 5)
-    res["kernels_ms"] = {"jacobi_f32": ms_j32, "fapply_f32": ms_a32, "jacobi_f64": ms_j64}
+    ms_a64 = op.time_sweep(0, "f64", 0, 5)
+    res["kernels_ms"] = {"jacobi_f32": ms_j32, "fapply_f32": ms_a32, "jacobi_f64": ms_j64, "fapply_f64": ms_a64}
     # the FP64 sweeps are bound by the FP64 pipe: its throughput, measured now
     from alamo_gb300.elastic import fp64_fma_peak
     res["fp64_peak_tflops"] = max(fp64_fma_peak()[0] for _ in range(3))
@@ -636,6 +637,8 @@ def main():
         "fapply_f32_gbs": round(BYTES_PER_NODE["fapply_f32_cubic"] * nodes / (res["kernels_ms"]["fapply_f32"] * 1e-3)
                                 / 1e9, 1),
         "jacobi_f64_gbs": round(BYTES_PER_NODE["jacobi_f64_cubic"] * nodes / (res["kernels_ms"]["jacobi_f64"] * 1e-3)
+                                / 1e9, 1),
+        "fapply_f64_gbs": round(BYTES_PER_NODE["fapply_f64_cubic"] * nodes / (res["kernels_ms"]["fapply_f64"] * 1e-3)
                                 / 1e9, 1),
         "kernel_ms": res["kernels_ms"],
         "fp64_roofline": {
