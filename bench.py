@@ -41,7 +41,7 @@ BYTES_PER_NODE = {"jacobi_f32_cubic": 132, "fapply_f32_cubic": 108, "jacobi_f64_
 # cells (an FMA counts 2), counted by ncu on the marching kernel (DFMA, DADD,
 # DMUL thread instructions over the interior nodes of one 65^3 launch:
 # 98 + 129 + 26)
-FLOPS_PER_NODE = {"jacobi_f64_cubic": 351}
+FLOPS_PER_NODE = {"jacobi_f64_cubic": 351, "fapply_f64_cubic": 339}   # Fapply: 95 + 126 + 23
 
 
 def parse():
@@ -648,7 +648,12 @@ def main():
                               / 1e12, 3),
             "peak": round(res["fp64_peak_tflops"], 3), "unit": "TFLOP/s", "peak_kind": "measured (FP64 FMA loop)",
             "frac": round(FLOPS_PER_NODE["jacobi_f64_cubic"] * nodes / (res["kernels_ms"]["jacobi_f64"] * 1e-3)
-                          / 1e12 / res["fp64_peak_tflops"], 4)},
+                          / 1e12 / res["fp64_peak_tflops"], 4),
+            "fapply": {"flops_per_node": FLOPS_PER_NODE["fapply_f64_cubic"],
+                       "achieved": round(FLOPS_PER_NODE["fapply_f64_cubic"] * nodes
+                                         / (res["kernels_ms"]["fapply_f64"] * 1e-3) / 1e12, 3),
+                       "frac": round(FLOPS_PER_NODE["fapply_f64_cubic"] * nodes
+                                     / (res["kernels_ms"]["fapply_f64"] * 1e-3) / 1e12 / res["fp64_peak_tflops"], 4)}},
         "mixed": res["mixed"],
     }
     if "plain" in res:
