@@ -169,3 +169,39 @@ def test_fp32_interior_apply_and_smooth(gpu_lib, case, sym, uniform):
     x = op.Fsmooth(0, u32.copy(), b32)
     xs = O.fsmooth(g, d32, O.diagonal(g, d32), u32.astype(np.float64), b32.astype(np.float64))
     assert rel_err(x.astype(np.float64), xs) < TOL32
+
+
+@pytest.mark.parametrize("sym", SYMS)
+def test_pinned_host_fields(gpu_lib, sym):
+    """Pinned host fields are read and written in place by the import and
+    export kernels (mapped addresses): SetModel, Fapply (FP64 and FP32) and
+    Fsmooth from and into pinned host buffers give the same values, bit for
+    bit, as from pageable ones."""
+    import torch
+    case = CASES[1]
+    op, g, ddw = make(case, sym, 31)
+    N = O.nodes(g)
+    rng = np.random.default_rng(32)
+    u = rng.uniform(-1, 1, 3 * N)
+    b = rng.uniform(-1, 1, 3 * N)
+
+    def pin(a):
+        return torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+
+    f_pageable = op.Fapply(0, u)
+    f_pinned = pin(np.zeros(3 * N))
+    op.Fapply(0, pin(u), out=f_pinned)
+    assert np.array_equal(f_pinned, f_pageable)
+    x_pageable = op.Fsmooth(0, u.copy(), b)
+    x_pinned = pin(u)
+    op.Fsmooth(0, x_pinned, pin(b))
+    assert np.array_equal(x_pinned, x_pageable)
+    op.SetModel(pin(ddw))
+    assert np.array_equal(op.GetModel(0), ddw)
+    assert np.array_equal(op.Fapply(0, u), f_pageable)
+    u32 = u.astype(np.float32)
+    f32 = op.Fapply(0, u32)
+    f32_pinned = torch.zeros(3 * N, dtype=torch.float32).pin_memory().numpy()
+    op.Fapply(0, torch.from_numpy(u32).pin_memory().numpy(), out=f32_pinned)
+    assert np.array_equal(f32_pinned, f32)
+    op.close()
