@@ -569,7 +569,14 @@ static void stencil_dispatch(cudaStream_t st, const LevelDesc& L, const BCTable&
         count_launch();
     } else {
         dim3 b2(32, 4, 2);
-        if (L.nn[0] <= 16) b2 = dim3(8, 8, 4);
+        // rows of at most 40 nodes (the 33^3 and 17^3 levels of a 2^k box
+        // and below) in 8 x 8 x 4 blocks: fewer idle lanes than 32-wide rows
+        // (solve 0.3247 against 0.3258 s at 257^3); AGB_NODE_NARROW overrides
+        static const int narrow = [] {
+            const char* e = getenv("AGB_NODE_NARROW");
+            return e ? atoi(e) : 40;
+        }();
+        if (L.nn[0] <= narrow) b2 = dim3(8, 8, 4);
         pdl_launch(k_stencil_node<T, SYM, MODE>, node_grid(L, b2), b2, 0, st, L, bc, g, uniform ? 1 : 0, ddw, x, b,
                    diag, out, omega, norm_slot, 0);
         count_launch();
