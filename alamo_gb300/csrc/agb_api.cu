@@ -999,7 +999,7 @@ agb_status solve_mixed(agb_solver s, double tol_rel, double tol_abs, agb_solve_r
         if (std::isnan(norm)) { st = AGB_NAN; break; }
         if (norm <= target) { st = AGB_OK; break; }
         no_progress = (norm > 0.5 * old) ? no_progress + 1 : 0;
-        if (no_progress >= 1) s->learned_on = false;   // the FP64 residual is the judge: plain cycles from here
+        if (no_progress >= 1) s->learned_on = false;   // the FP64 residual decides: plain cycles from here
         if (no_progress >= 2) { st = AGB_STALL; break; }
     }
     rep->iterations = total_cycles;
